@@ -1,0 +1,349 @@
+// gpda_device.cuh — device-side random numbers, FP32 elementary functions and
+// samplers of the photon-burst Monte-Carlo PDA kernels (sm_103a).
+//
+// Everything here is deterministic FP32/INT32 arithmetic with a fixed
+// operation order. The kernels are compiled with -fmad=false, so no multiply-
+// add is contracted unless written as fmaf(); together with IEEE division and
+// square root this makes every sampling decision reproducible on the host.
+//
+// Random numbers: Philox4x32-10 (Salmon et al., SC'11) kept in registers. A
+// unit (parameter-set word, burst, sample) owns the counter space
+// (block, sample, burst, pword) under key = seed; this replaces the
+// reference's per-thread curandStateScrambledSobol64 + rk_state arrays in HBM
+// (src/gen_rand.cuh:7-25, src/mc.cu:366-454).
+#pragma once
+#include <cstdint>
+
+namespace gpda {
+
+constexpr int kMaxStates = 8;
+constexpr int kMaxSeg = 65536;      // segments per unit before the trajectory is cut
+constexpr int kMaxRestart = 256;    // rejection restarts before the sampler gives up
+
+// ---------------------------------------------------------------- Philox
+struct Rng {
+    uint32_t k0, k1, c1, c2, c3, blk;
+    uint32_t w0, w1, w2, w3;
+    int idx;
+
+    __device__ __forceinline__ void init(uint64_t seed, uint32_t pword, uint32_t b, uint32_t s) {
+        k0 = (uint32_t)seed;
+        k1 = (uint32_t)(seed >> 32);
+        c1 = s; c2 = b; c3 = pword;
+        blk = 0u;
+        idx = 4;
+    }
+    __device__ __forceinline__ void block() {
+        uint32_t x0 = blk, x1 = c1, x2 = c2, x3 = c3;
+        uint32_t a = k0, b = k1;
+#pragma unroll
+        for (int r = 0; r < 10; ++r) {
+            uint64_t p0 = (uint64_t)0xD2511F53u * x0;
+            uint64_t p1 = (uint64_t)0xCD9E8D57u * x2;
+            uint32_t n0 = (uint32_t)(p1 >> 32) ^ x1 ^ a;
+            uint32_t n2 = (uint32_t)(p0 >> 32) ^ x3 ^ b;
+            x1 = (uint32_t)p1;
+            x3 = (uint32_t)p0;
+            x0 = n0;
+            x2 = n2;
+            a += 0x9E3779B9u;
+            b += 0xBB67AE85u;
+        }
+        w0 = x0; w1 = x1; w2 = x2; w3 = x3;
+        blk += 1u;
+    }
+    __device__ __forceinline__ uint32_t next() {
+        if (idx == 4) { block(); idx = 0; }
+        uint32_t r = (idx == 0) ? w0 : (idx == 1) ? w1 : (idx == 2) ? w2 : w3;
+        ++idx;
+        return r;
+    }
+    // uniform on (0,1]: ((x >> 8) + 1) * 2^-24, exact
+    __device__ __forceinline__ float u01() {
+        return (float)((next() >> 8) + 1u) * 5.9604644775390625e-08f;
+    }
+};
+
+// ---------------------------------------------------------------- FP32 math
+// Written from the mathematics: log by 2*atanh((m-1)/(m+1)) series, exp by
+// Taylor series after k*ln2 reduction, cos(2*pi*u) by the sine series.
+constexpr float kLn2Hi = 0x1.62e430p-1f;
+constexpr float kLn2Lo = -0x1.05c610p-29f;
+constexpr float kLog2e = 0x1.715476p+0f;
+constexpr float kSqrt2 = 0x1.6a09e6p+0f;
+constexpr float kInf = __builtin_huge_valf();
+
+__device__ __forceinline__ float logf_(float x) {
+    if (x != x) return x;
+    if (x < 0.0f) return __int_as_float(0x7fc00000);
+    if (x == 0.0f) return -kInf;
+    if (x == kInf) return x;
+    uint32_t bits = __float_as_uint(x);
+    int e = 0;
+    if ((bits >> 23) == 0u) {
+        x = x * 0x1p24f;
+        bits = __float_as_uint(x);
+        e = -24;
+    }
+    e += (int)(bits >> 23) - 127;
+    float m = __uint_as_float((bits & 0x007FFFFFu) | 0x3F800000u);
+    if (m > kSqrt2) { m = m * 0.5f; e += 1; }
+    float f = m - 1.0f;
+    float s = f / (2.0f + f);
+    float z = s * s;
+    float poly = fmaf(z, fmaf(z, fmaf(z, 0x1.c71c72p-3f, 0x1.24924ap-2f), 0x1.99999ap-2f), 0x1.555556p-1f);
+    float lm = fmaf(s * z, poly, 2.0f * s);
+    float ef = (float)e;
+    return fmaf(ef, kLn2Hi, fmaf(ef, kLn2Lo, lm));
+}
+
+__device__ __forceinline__ float expf_(float x) {
+    if (x != x) return x;
+    if (x > 88.72284f) return kInf;
+    if (x < -103.97208f) return 0.0f;
+    float kf = rintf(x * kLog2e);
+    float r = fmaf(-kf, kLn2Hi, x);
+    r = fmaf(-kf, kLn2Lo, r);
+    float p = 0x1.a01a02p-13f;
+    p = fmaf(p, r, 0x1.6c16c2p-10f);
+    p = fmaf(p, r, 0x1.111112p-7f);
+    p = fmaf(p, r, 0x1.555556p-5f);
+    p = fmaf(p, r, 0x1.555556p-3f);
+    p = fmaf(p, r, 0.5f);
+    p = fmaf(p, r, 1.0f);
+    p = fmaf(p, r, 1.0f);
+    int k = (int)kf;
+    if (k >= -126 && k <= 127) return p * __uint_as_float((uint32_t)(k + 127) << 23);
+    int k1 = k / 2, k2 = k - k1;
+    return (p * __uint_as_float((uint32_t)(k1 + 127) << 23)) * __uint_as_float((uint32_t)(k2 + 127) << 23);
+}
+
+__device__ __forceinline__ float cos2pif_(float u) {
+    float w = (u > 0.5f) ? 1.0f - u : u;
+    float rr = 0.25f - w;
+    float th = rr * 0x1.921fb6p+2f;
+    float t2 = th * th;
+    float p = 0x1.612462p-33f;
+    p = fmaf(p, t2, -0x1.ae6456p-26f);
+    p = fmaf(p, t2, 0x1.71de3ap-19f);
+    p = fmaf(p, t2, -0x1.a01a02p-13f);
+    p = fmaf(p, t2, 0x1.111112p-7f);
+    p = fmaf(p, t2, -0x1.555556p-3f);
+    p = fmaf(p, t2, 1.0f);
+    return th * p;
+}
+
+// Stirling correction fc(k) = ln k! - ((k+1/2) ln(k+1) - (k+1) + ln(2 pi)/2), k < 10
+__device__ __forceinline__ float fc_tab(int k) {
+    switch (k) {
+    case 0: return 8.106146680e-02f; case 1: return 4.134069596e-02f;
+    case 2: return 2.767792568e-02f; case 3: return 2.079067210e-02f;
+    case 4: return 1.664469119e-02f; case 5: return 1.387612882e-02f;
+    case 6: return 1.189670995e-02f; case 7: return 1.041126526e-02f;
+    case 8: return 9.255462183e-03f; default: return 8.330563433e-03f;
+    }
+}
+__device__ __forceinline__ float lf_tab(int k) {
+    switch (k) {
+    case 0: return 0.0f; case 1: return 0.0f; case 2: return 0.693147182f;
+    case 3: return 1.791759491f; case 4: return 3.178053856f; case 5: return 4.787491798f;
+    case 6: return 6.579251289f; case 7: return 8.525161743f; case 8: return 10.60460281f;
+    default: return 12.80182743f;
+    }
+}
+__device__ __forceinline__ float fc(float k) {
+    if (k < 10.0f) return fc_tab((int)k);
+    float kp = k + 1.0f;
+    float k2 = kp * kp;
+    return (0.083333333333333333f - (0.0027777777777777778f - 0.00079365079365079365f / k2) / k2) / kp;
+}
+
+// ---------------------------------------------------------------- samplers
+// Binomial by sequential-search inversion (Kachitvichyanukul & Schmeiser
+// 1988); p <= 1/2, n p < 10.
+__device__ __noinline__ int binv(Rng &r, int n, float p, int &lim) {
+    float q = 1.0f - p;
+    float nf = (float)n;
+    float qn = expf_(nf * logf_(q));
+    float rr = p / q;
+    float g = rr * (nf + 1.0f);
+    float np = nf * p;
+    float bf = np + 10.0f * sqrtf(np * q + 1.0f);
+    int bound = (bf < nf) ? (int)bf : n;
+    for (int it = 0; it < kMaxRestart; ++it) {
+        int x = 0;
+        float f = qn;
+        float u = r.u01();
+        while (u > f) {
+            u = u - f;
+            x += 1;
+            if (x > bound) break;
+            f = f * (g / (float)x - rr);
+        }
+        if (x <= bound) return x;
+    }
+    lim += 1;
+    return (int)np;
+}
+
+// Binomial by transformed rejection with decomposition (Hoermann 1993,
+// BTRD); p <= 1/2, n p >= 10.
+__device__ __noinline__ int btrd(Rng &r, int n, float p, int &lim) {
+    float nf = (float)n;
+    float q = 1.0f - p;
+    float rr = p / q;
+    float nr = (nf + 1.0f) * rr;
+    float m = floorf((nf + 1.0f) * p);
+    float npq = nf * p * q;
+    float snpq = sqrtf(npq);
+    float b = 1.15f + 2.53f * snpq;
+    float a = -0.0873f + 0.0248f * b + 0.01f * p;
+    float c = nf * p + 0.5f;
+    float alpha = (2.83f + 5.1f / b) * snpq;
+    float vr = 0.92f - 4.2f / b;
+    float urvr = 0.86f * vr;
+    for (int it = 0; it < kMaxRestart; ++it) {
+        float v = r.u01();
+        float u;
+        if (v <= urvr) {
+            u = v / vr - 0.43f;
+            float kf = floorf((2.0f * a / (0.5f - fabsf(u)) + b) * u + c);
+            if (kf >= 0.0f && kf <= nf) return (int)kf;
+            continue;
+        }
+        if (v >= vr) {
+            u = r.u01() - 0.5f;
+        } else {
+            u = v / vr - 0.93f;
+            u = copysignf(0.5f, u) - u;
+            v = r.u01() * vr;
+        }
+        float us = 0.5f - fabsf(u);
+        if (!(us > 0.0f)) continue;
+        float kf = floorf((2.0f * a / us + b) * u + c);
+        if (!(kf >= 0.0f && kf <= nf)) continue;
+        v = v * alpha / (a / (us * us) + b);
+        float km = fabsf(kf - m);
+        if (km <= 15.0f) {
+            float f = 1.0f;
+            int k = (int)kf, mi = (int)m;
+            if (mi < k) {
+                for (int i = mi + 1; i <= k; ++i) f = f * (nr / (float)i - rr);
+            } else if (mi > k) {
+                for (int i = k + 1; i <= mi; ++i) v = v * (nr / (float)i - rr);
+            }
+            if (v <= f) return k;
+            continue;
+        }
+        v = logf_(v);
+        float rho = (km / npq) * (((km / 3.0f + 0.625f) * km + 0.16666666666666667f) / npq + 0.5f);
+        float t = -km * km / (2.0f * npq);
+        if (v < t - rho) return (int)kf;
+        if (v > t + rho) continue;
+        float nm = nf - m + 1.0f;
+        float h = (m + 0.5f) * logf_((m + 1.0f) / (rr * nm)) + fc(m) + fc(nf - m);
+        float nk = nf - kf + 1.0f;
+        float bound = h + (nf + 1.0f) * logf_(nm / nk) + (kf + 0.5f) * logf_(nk * rr / (kf + 1.0f))
+                      - fc(kf) - fc(nf - kf);
+        if (v <= bound) return (int)kf;
+    }
+    lim += 1;
+    return (int)m;
+}
+
+__device__ __forceinline__ int binom(Rng &r, int n, float p, int &lim) {
+    if (n <= 0 || !(p > 0.0f)) return 0;
+    if (p >= 1.0f) return n;
+    bool flip = p > 0.5f;
+    float pp = flip ? 1.0f - p : p;
+    int x = ((float)n * pp < 10.0f) ? binv(r, n, pp, lim) : btrd(r, n, pp, lim);
+    return flip ? n - x : x;
+}
+
+// Poisson by sequential-search inversion, lam < 10.
+__device__ __forceinline__ int pinv(Rng &r, float lam, int &lim) {
+    float L = expf_(-lam);
+    int bound = (int)(lam + 10.0f * sqrtf(lam) + 10.0f);
+    for (int it = 0; it < kMaxRestart; ++it) {
+        int k = 0;
+        float f = L;
+        float u = r.u01();
+        while (u > f) {
+            u = u - f;
+            k += 1;
+            if (k > bound) break;
+            f = (f * lam) / (float)k;
+        }
+        if (k <= bound) return k;
+    }
+    lim += 1;
+    return (int)lam;
+}
+
+__device__ __forceinline__ float logfact(float k) {
+    if (k < 10.0f) return lf_tab((int)k);
+    return (k + 0.5f) * logf_(k + 1.0f) - (k + 1.0f) + 0.91893853320467274f + fc(k);
+}
+
+// Poisson by transformed rejection with squeeze (Hoermann 1993, PTRS), lam >= 10.
+__device__ __noinline__ int ptrs(Rng &r, float lam, int &lim) {
+    float slam = sqrtf(lam);
+    float loglam = logf_(lam);
+    float b = 0.931f + 2.53f * slam;
+    float a = -0.059f + 0.02483f * b;
+    float invalpha = 1.1239f + 1.1328f / (b - 3.4f);
+    float vr = 0.9277f - 3.6224f / (b - 2.0f);
+    float lia = logf_(invalpha);
+    for (int it = 0; it < kMaxRestart; ++it) {
+        float U = r.u01() - 0.5f;
+        float V = r.u01();
+        float us = 0.5f - fabsf(U);
+        if (!(us > 0.0f)) continue;
+        float kf = floorf((2.0f * a / us + b) * U + lam + 0.43f);
+        if (us >= 0.07f && V <= vr) {
+            if (kf >= 0.0f && kf < 2.0e9f) return (int)kf;
+            continue;
+        }
+        if (!(kf >= 0.0f && kf < 2.0e9f)) continue;
+        if (us < 0.013f && V > us) continue;
+        float lhs = logf_(V) + lia - logf_(a / (us * us) + b);
+        float rhs = -lam + kf * loglam - logfact(kf);
+        if (lhs <= rhs) return (int)kf;
+    }
+    lim += 1;
+    return (int)lam;
+}
+
+__device__ __forceinline__ int poisson(Rng &r, float lam, int &lim) {
+    if (!(lam > 0.0f)) return 0;
+    return (lam < 10.0f) ? pinv(r, lam, lim) : ptrs(r, lam, lim);
+}
+
+__device__ __forceinline__ float normal(Rng &r) {
+    float u1 = r.u01();
+    float u2 = r.u01();
+    return sqrtf(-2.0f * logf_(u1)) * cos2pif_(u2);
+}
+
+__device__ __forceinline__ float root6(float x) {
+    if (!(x > 0.0f)) return (x == 0.0f) ? 0.0f : __int_as_float(0x7fc00000);
+    return expf_(logf_(x) * 0.16666666666666667f);
+}
+
+// drawE (src/gen_rand.cuh:63-68): distance-broadened efficiency
+__device__ __noinline__ float broaden(Rng &r, float e, float r0, float v) {
+    float z = normal(r);
+    float rd = z * v + r0 * root6(1.0f / e - 1.0f);
+    float t = rd / r0;
+    float t2 = t * t;
+    float t6 = (t2 * t2) * t2;
+    return 1.0f / (1.0f + t6);
+}
+
+__device__ __forceinline__ float eps_of(float e, float g, float ct) {
+    float om = 1.0f - e;
+    float num = g * e + ct * om;
+    return num / (num + om);
+}
+
+}  // namespace gpda

@@ -1,0 +1,446 @@
+// gpda_engine.cu — host engine and C ABI of the pda model (include/gpda.h).
+//
+// One context = one device + one CUDA stream + a burst store resident in HBM:
+//   N        int32[B]        photons per burst
+//   T        float[B]        burst duration (s)
+//   off_idx  int64[B+1]      prefix offsets (photon mode)
+//   offsets  float[sum N + pad] sorted arrival offsets, padded so that the
+//                            kernels can read whole 16-byte vectors
+// Per launch: P parameter-set tables (DevParams, staged through pinned
+// memory), a P x nbins uint64 histogram, P chi-square values.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/gpda.h"
+#include "gpda_internal.h"
+
+using namespace gpda;
+
+struct gpda_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t params_ev = nullptr;
+    gpda_model model{};
+    int num_sms = 0;
+    // burst store
+    int64_t B = 0;
+    int64_t nph = 0;
+    double mean_N = 0.0;
+    int32_t *dN = nullptr;
+    float *dT = nullptr;
+    int64_t *dOffIdx = nullptr;
+    float *dOff = nullptr;
+    bool has_offsets = false;
+    // observed histogram
+    float *dObs = nullptr;
+    bool has_obs = false;
+    // launch scratch
+    DevParams *dParams = nullptr;
+    DevParams *hParams = nullptr;  // pinned
+    int cap_P = 0;
+    unsigned long long *dHist = nullptr;
+    unsigned long long *hHist = nullptr;  // pinned
+    double *dChi2 = nullptr;
+    double *hChi2 = nullptr;  // pinned
+    int cap_hist = 0;
+    unsigned int *dWork = nullptr;
+    unsigned long long *dLimit = nullptr;
+    int32_t *dUnit = nullptr;
+    size_t cap_unit = 0;
+    // last launch
+    int last_P = 0;
+    bool last_chi2 = false;
+    int64_t launches = 0;
+    int blocks_per_sm[2] = {0, 0};
+    std::string err;
+};
+
+namespace {
+
+constexpr int kSmemCapFloats = 8192;  // photon staging: 32 KB of dynamic shared memory
+constexpr int kOffPad = 8;            // floats of padding behind the offsets array
+
+int fail(gpda_ctx *c, int code, const std::string &msg) {
+    if (c) c->err = msg;
+    return code;
+}
+
+int cuda_fail(gpda_ctx *c, cudaError_t e, const char *what) {
+    return fail(c, GPDA_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(call)                                             \
+    do {                                                     \
+        cudaError_t e_ = (call);                             \
+        if (e_ != cudaSuccess) return cuda_fail(c, e_, #call); \
+    } while (0)
+
+void free_dev(void *p) {
+    if (p) cudaFree(p);
+}
+
+int check_model(const gpda_model *m) {
+    if (!m) return -1;
+    if (m->nbins < 1 || m->nbins > GPDA_MAX_BINS) return -1;
+    if (m->left_pad < 0 || m->left_pad > m->nbins) return -1;
+    if (!(m->gamma > 0.0f && std::isfinite(m->gamma))) return -1;
+    if (!(m->crosstalk >= 0.0f && std::isfinite(m->crosstalk))) return -1;
+    if (!(m->bg_d >= 0.0f && std::isfinite(m->bg_d))) return -1;
+    if (!(m->bg_a >= 0.0f && std::isfinite(m->bg_a))) return -1;
+    if (!(m->r0 > 0.0f && m->rc_r0 > 0.0f)) return -1;
+    return 0;
+}
+
+int ensure_scratch(gpda_ctx *c, int P) {
+    int nb = c->model.nbins;
+    if (P > c->cap_P) {
+        free_dev(c->dParams);
+        if (c->hParams) cudaFreeHost(c->hParams);
+        c->dParams = nullptr;
+        c->hParams = nullptr;
+        c->cap_P = 0;
+        CK(cudaMalloc(&c->dParams, sizeof(DevParams) * (size_t)P));
+        CK(cudaMallocHost(&c->hParams, sizeof(DevParams) * (size_t)P));
+        c->cap_P = P;
+    }
+    if (P * nb > c->cap_hist) {
+        free_dev(c->dHist);
+        free_dev(c->dChi2);
+        if (c->hHist) cudaFreeHost(c->hHist);
+        if (c->hChi2) cudaFreeHost(c->hChi2);
+        c->dHist = nullptr; c->dChi2 = nullptr; c->hHist = nullptr; c->hChi2 = nullptr;
+        c->cap_hist = 0;
+        CK(cudaMalloc(&c->dHist, sizeof(unsigned long long) * (size_t)P * nb));
+        CK(cudaMalloc(&c->dChi2, sizeof(double) * (size_t)P));
+        CK(cudaMallocHost(&c->hHist, sizeof(unsigned long long) * (size_t)P * nb));
+        CK(cudaMallocHost(&c->hChi2, sizeof(double) * (size_t)P));
+        c->cap_hist = P * nb;
+    }
+    return GPDA_OK;
+}
+
+int tile_bursts(const gpda_ctx *c, int mode, int S) {
+    int tb = (2048 + S - 1) / S;
+    if (mode == GPDA_MODE_PHOTON && c->mean_N > 0.0) {
+        int fit = (int)(0.6 * kSmemCapFloats / c->mean_N);
+        tb = std::min(tb, std::max(fit, 1));
+    }
+    return std::max(1, std::min(tb, kMaxTileBursts));
+}
+
+int do_launch(gpda_ctx *c, int mode, int P, int n, const float *params, int64_t b0, int64_t b1,
+              int S, uint64_t seed, int32_t *dUnit) {
+    if (mode != GPDA_MODE_OCCUPANCY && mode != GPDA_MODE_PHOTON) return fail(c, GPDA_ERR_ARG, "mode");
+    if (P < 1 || n < 1 || n > GPDA_MAX_STATES || S < 1 || !params) return fail(c, GPDA_ERR_ARG, "P, n_states, samples or params");
+    if (c->B == 0 || !c->dN) return fail(c, GPDA_ERR_STATE, "no bursts uploaded");
+    if (b0 < 0 || b1 < b0 || b1 > c->B) return fail(c, GPDA_ERR_ARG, "burst range");
+    if (mode == GPDA_MODE_PHOTON && !c->has_offsets) return fail(c, GPDA_ERR_STATE, "photon mode needs arrival offsets");
+    if ((int64_t)(b1 - b0) * S > (int64_t)INT32_MAX) return fail(c, GPDA_ERR_ARG, "too many units per parameter set");
+    CK(cudaSetDevice(c->device));
+    int rc = ensure_scratch(c, P);
+    if (rc) return rc;
+    // the pinned parameter staging may still be read by the previous copy
+    CK(cudaEventSynchronize(c->params_ev));
+    const size_t stride = (size_t)n * (n + 1);
+    for (int p = 0; p < P; ++p) {
+        int r = build_params(n, params + stride * p, c->model.gamma, c->model.crosstalk, true, &c->hParams[p]);
+        if (r == -2) return fail(c, GPDA_ERR_SINGULAR, "rate matrix has no unique stationary distribution (parameter set " + std::to_string(p) + ")");
+        if (r != 0) return fail(c, GPDA_ERR_ARG, "invalid parameter vector " + std::to_string(p));
+    }
+    const int nbins = c->model.nbins;
+    CK(cudaMemcpyAsync(c->dParams, c->hParams, sizeof(DevParams) * P, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaEventRecord(c->params_ev, c->stream));
+    CK(cudaMemsetAsync(c->dHist, 0, sizeof(unsigned long long) * (size_t)P * nbins, c->stream));
+    CK(cudaMemsetAsync(c->dWork, 0, sizeof(unsigned int), c->stream));
+    c->last_P = P;
+    c->last_chi2 = false;
+    if (b1 == b0) return GPDA_OK;
+    PdaArgs a{};
+    a.N = c->dN;
+    a.T = c->dT;
+    a.off_idx = c->dOffIdx;
+    a.offsets = c->dOff;
+    a.params = c->dParams;
+    a.hist = c->dHist;
+    a.unit_out = dUnit;
+    a.work = c->dWork;
+    a.limit_hits = c->dLimit;
+    a.b0 = b0;
+    a.b1 = b1;
+    a.seed = seed;
+    a.P = P;
+    a.S = S;
+    a.tile_b = tile_bursts(c, mode, S);
+    int64_t ntiles = (b1 - b0 + a.tile_b - 1) / a.tile_b;
+    if (ntiles * P > (int64_t)INT32_MAX) return fail(c, GPDA_ERR_ARG, "too many work items");
+    a.ntiles = (int)ntiles;
+    a.n_items = (int)(ntiles * P);
+    a.nbins = nbins;
+    a.smem_cap = kSmemCapFloats;
+    a.pbase = 0u;
+    a.gamma = c->model.gamma;
+    a.ct = c->model.crosstalk;
+    a.r0 = c->model.r0;
+    a.bg_a = c->model.bg_a;
+    a.bg_d = c->model.bg_d;
+    size_t dyn = (mode == GPDA_MODE_PHOTON) ? sizeof(float) * kSmemCapFloats : 0;
+    int grid = std::min<int64_t>(a.n_items, (int64_t)c->num_sms * c->blocks_per_sm[mode]);
+    CK(launch_pda(mode, a, grid, dyn, c->stream));
+    c->launches += 1;
+    if (c->has_obs) {
+        CK(launch_chi2(c->dHist, c->dObs, P, nbins, c->model.left_pad, S, n, c->dChi2, c->stream));
+        c->launches += 1;
+        c->last_chi2 = true;
+    }
+    return GPDA_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void gpda_model_defaults(gpda_model *m) {
+    m->nbins = 21;
+    m->left_pad = 2;
+    m->gamma = 1.0f;
+    m->crosstalk = 0.05f;
+    m->bg_d = 1500.0f;
+    m->bg_a = 800.0f;
+    m->r0 = 52.0f;
+    m->rc_gamma = 0.34f;
+    m->rc_de = 0.08f;
+    m->rc_ct = 0.07f;
+    m->rc_r0 = 52.0f;
+}
+
+const char *gpda_version(void) { return "gpda 0.1 sm_103a"; }
+
+gpda_ctx *gpda_create(int32_t device, const gpda_model *m, int32_t *status) {
+    auto set = [&](int s) { if (status) *status = s; };
+    gpda_model mm;
+    if (m) mm = *m; else gpda_model_defaults(&mm);
+    if (check_model(&mm)) { set(GPDA_ERR_ARG); return nullptr; }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) {
+        cudaGetLastError();
+        set(GPDA_ERR_CUDA);
+        return nullptr;
+    }
+    gpda_ctx *c = new gpda_ctx();
+    c->device = device;
+    c->model = mm;
+    auto bad = [&](cudaError_t e) {
+        if (e == cudaSuccess) return false;
+        set(GPDA_ERR_CUDA);
+        gpda_destroy(c);
+        return true;
+    };
+    if (bad(cudaSetDevice(device))) return nullptr;
+    if (bad(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking))) return nullptr;
+    if (bad(cudaEventCreateWithFlags(&c->params_ev, cudaEventDisableTiming))) return nullptr;
+    if (bad(cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device))) return nullptr;
+    if (bad(cudaMalloc(&c->dWork, sizeof(unsigned int)))) return nullptr;
+    if (bad(cudaMalloc(&c->dLimit, sizeof(unsigned long long)))) return nullptr;
+    if (bad(cudaMemset(c->dLimit, 0, sizeof(unsigned long long)))) return nullptr;
+    if (bad(cudaMalloc(&c->dObs, sizeof(float) * GPDA_MAX_BINS))) return nullptr;
+    if (bad(cudaEventRecord(c->params_ev, c->stream))) return nullptr;
+    if (bad(pda_occupancy_blocks(0, 0, &c->blocks_per_sm[0]))) return nullptr;
+    if (bad(pda_occupancy_blocks(1, sizeof(float) * kSmemCapFloats, &c->blocks_per_sm[1]))) return nullptr;
+    for (int i = 0; i < 2; ++i) c->blocks_per_sm[i] = std::max(1, c->blocks_per_sm[i]);
+    set(GPDA_OK);
+    return c;
+}
+
+void gpda_destroy(gpda_ctx *c) {
+    if (!c) return;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    free_dev(c->dN); free_dev(c->dT); free_dev(c->dOffIdx); free_dev(c->dOff);
+    free_dev(c->dObs); free_dev(c->dParams); free_dev(c->dHist); free_dev(c->dChi2);
+    free_dev(c->dWork); free_dev(c->dLimit); free_dev(c->dUnit);
+    if (c->hParams) cudaFreeHost(c->hParams);
+    if (c->hHist) cudaFreeHost(c->hHist);
+    if (c->hChi2) cudaFreeHost(c->hChi2);
+    if (c->params_ev) cudaEventDestroy(c->params_ev);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+const char *gpda_last_error(const gpda_ctx *c) { return c ? c->err.c_str() : "null context"; }
+
+int32_t gpda_upload_bursts(gpda_ctx *c, const int32_t *N, const float *T, const int64_t *off_idx,
+                           const float *offsets, int64_t B) {
+    if (!c) return GPDA_ERR_ARG;
+    if (B < 1 || B > (int64_t)INT32_MAX || !N || !T) return fail(c, GPDA_ERR_ARG, "B, N or T");
+    if ((off_idx == nullptr) != (offsets == nullptr)) return fail(c, GPDA_ERR_ARG, "off_idx and offsets go together");
+    double sumN = 0.0;
+    for (int64_t b = 0; b < B; ++b) {
+        if (N[b] < 0 || N[b] > (1 << 21)) return fail(c, GPDA_ERR_ARG, "N out of [0, 2^21] at burst " + std::to_string(b));
+        if (!(T[b] >= 0.0f) || !std::isfinite(T[b])) return fail(c, GPDA_ERR_ARG, "T not finite and >= 0 at burst " + std::to_string(b));
+        sumN += N[b];
+    }
+    int64_t nph = 0;
+    if (off_idx) {
+        if (off_idx[0] != 0) return fail(c, GPDA_ERR_ARG, "off_idx[0] must be 0");
+        for (int64_t b = 0; b < B; ++b) {
+            if (off_idx[b + 1] - off_idx[b] != (int64_t)N[b]) return fail(c, GPDA_ERR_ARG, "off_idx inconsistent with N at burst " + std::to_string(b));
+            for (int64_t i = off_idx[b]; i < off_idx[b + 1]; ++i) {
+                if (!std::isfinite(offsets[i])) return fail(c, GPDA_ERR_ARG, "offset not finite");
+                if (i > off_idx[b] && offsets[i] < offsets[i - 1]) return fail(c, GPDA_ERR_ARG, "offsets not sorted in burst " + std::to_string(b));
+            }
+        }
+        nph = off_idx[B];
+    }
+    CK(cudaSetDevice(c->device));
+    CK(cudaStreamSynchronize(c->stream));
+    free_dev(c->dN); free_dev(c->dT); free_dev(c->dOffIdx); free_dev(c->dOff);
+    c->dN = nullptr; c->dT = nullptr; c->dOffIdx = nullptr; c->dOff = nullptr;
+    c->B = 0;
+    CK(cudaMalloc(&c->dN, sizeof(int32_t) * B));
+    CK(cudaMalloc(&c->dT, sizeof(float) * B));
+    CK(cudaMemcpyAsync(c->dN, N, sizeof(int32_t) * B, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->dT, T, sizeof(float) * B, cudaMemcpyHostToDevice, c->stream));
+    c->has_offsets = off_idx != nullptr;
+    if (off_idx) {
+        CK(cudaMalloc(&c->dOffIdx, sizeof(int64_t) * (B + 1)));
+        CK(cudaMalloc(&c->dOff, sizeof(float) * (nph + kOffPad)));
+        CK(cudaMemcpyAsync(c->dOffIdx, off_idx, sizeof(int64_t) * (B + 1), cudaMemcpyHostToDevice, c->stream));
+        CK(cudaMemsetAsync(c->dOff + nph, 0, sizeof(float) * kOffPad, c->stream));
+        if (nph > 0) CK(cudaMemcpyAsync(c->dOff, offsets, sizeof(float) * nph, cudaMemcpyHostToDevice, c->stream));
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    c->B = B;
+    c->nph = nph;
+    c->mean_N = sumN / (double)B;
+    return GPDA_OK;
+}
+
+int32_t gpda_set_observed(gpda_ctx *c, const float *ohist, int32_t nbins) {
+    if (!c) return GPDA_ERR_ARG;
+    if (!ohist || nbins != c->model.nbins) return fail(c, GPDA_ERR_ARG, "observed histogram must have model.nbins bins");
+    CK(cudaSetDevice(c->device));
+    CK(cudaMemcpyAsync(c->dObs, ohist, sizeof(float) * nbins, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    c->has_obs = true;
+    return GPDA_OK;
+}
+
+int32_t gpda_bin_values(const float *x, int64_t n, int32_t nbins, float *hist_out) {
+    if ((!x && n > 0) || n < 0 || !hist_out || nbins < 1) return GPDA_ERR_ARG;
+    for (int i = 0; i < nbins; ++i) hist_out[i] = 0.0f;
+    for (int64_t k = 0; k < n; ++k) {
+        double z = (double)x[k];
+        if (z < 1.0 && z >= 0.0) hist_out[(int)(z * (double)nbins)] += 1.0f;
+    }
+    return GPDA_OK;
+}
+
+int32_t gpda_params_size(void) { return kParamWords; }
+
+int32_t gpda_build_params(const gpda_model *m, int32_t n, const float *args, float *out) {
+    gpda_model mm;
+    if (m) mm = *m; else gpda_model_defaults(&mm);
+    if (!out) return GPDA_ERR_ARG;
+    DevParams p;
+    int r = build_params(n, args, mm.gamma, mm.crosstalk, true, &p);
+    if (r == -2) return GPDA_ERR_SINGULAR;
+    if (r != 0) return GPDA_ERR_ARG;
+    std::memcpy(out, &p, sizeof(p));
+    return GPDA_OK;
+}
+
+int32_t gpda_launch(gpda_ctx *c, int32_t mode, int32_t P, int32_t n, const float *params,
+                    int64_t b0, int64_t b1, int32_t S, uint64_t seed) {
+    if (!c) return GPDA_ERR_ARG;
+    return do_launch(c, mode, P, n, params, b0, b1, S, seed, nullptr);
+}
+
+int32_t gpda_fetch(gpda_ctx *c, uint64_t *hist_out, double *chi2_out) {
+    if (!c) return GPDA_ERR_ARG;
+    if (c->last_P == 0) return fail(c, GPDA_ERR_STATE, "nothing launched");
+    CK(cudaSetDevice(c->device));
+    const int P = c->last_P, nb = c->model.nbins;
+    if (hist_out) CK(cudaMemcpyAsync(c->hHist, c->dHist, sizeof(unsigned long long) * (size_t)P * nb, cudaMemcpyDeviceToHost, c->stream));
+    if (chi2_out && c->last_chi2) CK(cudaMemcpyAsync(c->hChi2, c->dChi2, sizeof(double) * P, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (hist_out) std::memcpy(hist_out, c->hHist, sizeof(uint64_t) * (size_t)P * nb);
+    if (chi2_out) {
+        if (c->last_chi2) std::memcpy(chi2_out, c->hChi2, sizeof(double) * P);
+        else for (int p = 0; p < P; ++p) chi2_out[p] = NAN;
+    }
+    return GPDA_OK;
+}
+
+int32_t gpda_run_plain(gpda_ctx *c, int32_t mode, int32_t n, const float *params, int64_t b0,
+                       int64_t b1, int32_t S, uint64_t seed, uint64_t *hist_out, double *chi2_out) {
+    if (!c) return GPDA_ERR_ARG;
+    int r = do_launch(c, mode, 1, n, params, b0, b1, S, seed, nullptr);
+    if (r) return r;
+    return gpda_fetch(c, hist_out, chi2_out);
+}
+
+int32_t gpda_run_batched(gpda_ctx *c, int32_t mode, int32_t P, int32_t n, const float *params,
+                         int32_t S, uint64_t seed, uint64_t *hist_out, double *chi2_out) {
+    if (!c) return GPDA_ERR_ARG;
+    int r = do_launch(c, mode, P, n, params, 0, c->B, S, seed, nullptr);
+    if (r) return r;
+    return gpda_fetch(c, hist_out, chi2_out);
+}
+
+int32_t gpda_run_units(gpda_ctx *c, int32_t mode, int32_t P, int32_t n, const float *params,
+                       int64_t b0, int64_t b1, int32_t S, uint64_t seed, int32_t *unit_out,
+                       uint64_t *hist_out) {
+    if (!c) return GPDA_ERR_ARG;
+    if (!unit_out || b1 < b0 || P < 1 || S < 1) return fail(c, GPDA_ERR_ARG, "unit_out, range, P or S");
+    size_t cnt = (size_t)P * (size_t)(b1 - b0) * (size_t)S;
+    CK(cudaSetDevice(c->device));
+    if (cnt > c->cap_unit) {
+        CK(cudaStreamSynchronize(c->stream));
+        free_dev(c->dUnit);
+        c->dUnit = nullptr;
+        c->cap_unit = 0;
+        CK(cudaMalloc(&c->dUnit, sizeof(int32_t) * std::max<size_t>(cnt, 1)));
+        c->cap_unit = cnt;
+    }
+    int r = do_launch(c, mode, P, n, params, b0, b1, S, seed, c->dUnit);
+    if (r) return r;
+    if (cnt) CK(cudaMemcpyAsync(unit_out, c->dUnit, sizeof(int32_t) * cnt, cudaMemcpyDeviceToHost, c->stream));
+    return gpda_fetch(c, hist_out, nullptr);
+}
+
+int32_t gpda_query(gpda_ctx *c) {
+    if (!c) return GPDA_ERR_ARG;
+    cudaSetDevice(c->device);
+    cudaError_t e = cudaStreamQuery(c->stream);
+    if (e == cudaSuccess) return 1;
+    if (e == cudaErrorNotReady) return 0;
+    return cuda_fail(c, e, "cudaStreamQuery");
+}
+
+int32_t gpda_synchronize(gpda_ctx *c) {
+    if (!c) return GPDA_ERR_ARG;
+    CK(cudaSetDevice(c->device));
+    CK(cudaStreamSynchronize(c->stream));
+    return GPDA_OK;
+}
+
+void *gpda_stream(gpda_ctx *c) { return c ? (void *)c->stream : nullptr; }
+
+int64_t gpda_launch_count(const gpda_ctx *c) { return c ? c->launches : 0; }
+
+int64_t gpda_limit_hits(gpda_ctx *c) {
+    if (!c) return GPDA_ERR_ARG;
+    unsigned long long v = 0;
+    cudaSetDevice(c->device);
+    if (cudaMemcpyAsync(&v, c->dLimit, sizeof(v), cudaMemcpyDeviceToHost, c->stream) != cudaSuccess) return GPDA_ERR_CUDA;
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess) return GPDA_ERR_CUDA;
+    return (int64_t)v;
+}
+
+}  // extern "C"

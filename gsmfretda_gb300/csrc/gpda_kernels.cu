@@ -1,0 +1,409 @@
+// gpda_kernels.cu — sm_103a kernels of the photon-burst Monte-Carlo PDA path.
+//
+//   pda_kernel<MODE>   persistent CTAs pull (parameter set, burst tile) work
+//                      items from an atomic counter; the tile's photon counts,
+//                      durations and (photon mode) arrival offsets are staged
+//                      in shared memory with 16-byte vector loads; each thread
+//                      simulates (burst, sample) units and bins the proximity
+//                      ratio into a shared-memory histogram with warp-
+//                      aggregated atomics; the histogram is flushed once per
+//                      work item. MODE 0: occupancy-weighted E, one binomial
+//                      split per unit. MODE 1: photon-by-photon state
+//                      assignment, one binomial per dwell segment.
+//   chi2_kernel        reduced chi-square per parameter set in FP64,
+//                      sequential over bins (src/streamWorker.cpp:197-206).
+//   rc_kernel          mc_kernel's semantics (src/mc.cu:83-197), one thread
+//                      per (burst, sample), fused with the reference's
+//                      histogram binning (src/streamWorker.cpp:33-38).
+//
+// No tensor cores: nothing here is a contraction. The work is INT32 (Philox)
+// and FP32 ALU bound; HBM traffic is the burst store read once per item.
+#include "gpda_device.cuh"
+#include "gpda_internal.h"
+
+namespace gpda {
+
+__device__ __forceinline__ int cat_draw(const float *cdf, int n, float u) {
+    for (int i = 0; i < n; ++i)
+        if (u <= cdf[i]) return i;
+    return n - 1;
+}
+
+__device__ __forceinline__ int jump_draw(const float *row, int n, int from, float u) {
+    int last = from;
+    for (int i = 0; i < n; ++i) {
+        if (i == from) continue;
+        last = i;
+        if (u <= row[i]) return i;
+    }
+    return last;
+}
+
+// number of offsets < x in the sorted range a[lo, hi)
+__device__ __forceinline__ int lower_bound(const float *a, int lo, int hi, float x) {
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (a[mid] < x) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+
+// Occupancy mode unit: Gillespie trajectory over [0,T] starting from the
+// stationary distribution, dwell = -ln(u)/k_exit, next state from the K
+// column; E_eff = sum_s f_s E_s; Poisson background (clipped), binomial split.
+__device__ __forceinline__ int unit_occ(const DevParams &P, float g, float ct, float r0,
+                                        float bga, float bgd, int Nb, float Tb, uint64_t seed,
+                                        uint32_t pw, uint32_t b, uint32_t s, int &lim) {
+    if (Nb <= 0) return -1;
+    Rng r;
+    r.init(seed, pw, b, s);
+    const int n = P.n;
+    int st = cat_draw(P.init_cdf, n, r.u01());
+    float eeff;
+    if (Tb > 0.0f) {
+        float t = 0.0f, acc = 0.0f;
+        for (int seg = 0;; ++seg) {
+            float u = r.u01();
+            float tau = (P.kexit[st] > 0.0f) ? (-logf_(u)) * P.inv_kexit[st] : kInf;
+            float tn = t + tau;
+            bool cut = seg == kMaxSeg - 1;
+            bool last = !(tn < Tb) || cut;
+            if (cut && tn < Tb) lim += 1;
+            float dt = last ? Tb - t : tn - t;
+            float es = P.E[st];
+            if (P.V[st] > 0.0f) es = broaden(r, es, r0, P.V[st]);
+            acc = fmaf(dt, es, acc);
+            if (last) break;
+            t = tn;
+            st = jump_draw(P.jump_cdf + st * 8, n, st, r.u01());
+        }
+        eeff = acc / Tb;
+    } else {
+        eeff = P.E[st];
+    }
+    int Ba = poisson(r, bga * Tb, lim);
+    if (Ba > Nb) Ba = (int)floorf((float)Nb * r.u01());
+    int rem = Nb - Ba;
+    int Bd = poisson(r, bgd * Tb, lim);
+    if (Bd > rem) Bd = (int)floorf((float)rem * r.u01());
+    int ns = rem - Bd;
+    return binom(r, ns, eps_of(eeff, g, ct), lim) + Ba;
+}
+
+// Photon mode unit: each photon takes the state at its arrival offset; per
+// dwell segment with photons, Poisson background then Binomial(signal, eps).
+__device__ __forceinline__ int unit_pho(const DevParams &P, float g, float ct, float r0,
+                                        float bga, float bgd, int Nb, float Tb,
+                                        const float *offs, uint64_t seed, uint32_t pw,
+                                        uint32_t b, uint32_t s, int &lim) {
+    if (Nb <= 0) return -1;
+    Rng r;
+    r.init(seed, pw, b, s);
+    const int n = P.n;
+    int st = cat_draw(P.init_cdf, n, r.u01());
+    float t = 0.0f;
+    int lo = 0, A = 0;
+    for (int seg = 0;; ++seg) {
+        float u = r.u01();
+        float tau = (P.kexit[st] > 0.0f) ? (-logf_(u)) * P.inv_kexit[st] : kInf;
+        float tn = t + tau;
+        bool cut = seg == kMaxSeg - 1;
+        bool last = !(tn < Tb) || cut;
+        if (cut && tn < Tb) lim += 1;
+        int hi;
+        float dt;
+        if (last) { hi = Nb; dt = Tb - t; }
+        else { hi = lower_bound(offs, lo, Nb, tn); dt = tn - t; }
+        int nk = hi - lo;
+        if (nk > 0) {
+            float ek = P.eps[st];
+            if (P.V[st] > 0.0f) ek = eps_of(broaden(r, P.E[st], r0, P.V[st]), g, ct);
+            int Ba = poisson(r, bga * dt, lim);
+            if (Ba > nk) Ba = (int)floorf((float)nk * r.u01());
+            int rem = nk - Ba;
+            int Bd = poisson(r, bgd * dt, lim);
+            if (Bd > rem) Bd = (int)floorf((float)rem * r.u01());
+            A += binom(r, rem - Bd, ek, lim) + Ba;
+        }
+        lo = hi;
+        if (last) break;
+        t = tn;
+        st = jump_draw(P.jump_cdf + st * 8, n, st, r.u01());
+    }
+    return A;
+}
+
+// warp-aggregated shared-memory histogram increment (bin < 0: no count)
+__device__ __forceinline__ void hist_add(unsigned int *sh, int bin) {
+    unsigned mask = __activemask();
+    unsigned peers = __match_any_sync(mask, bin);
+    int leader = __ffs(peers) - 1;
+    if ((int)(threadIdx.x & 31) == leader && bin >= 0) atomicAdd(&sh[bin], (unsigned)__popc(peers));
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(kThreads) pda_kernel(const PdaArgs a) {
+    extern __shared__ float4 s_ph4[];
+    float *s_ph = reinterpret_cast<float *>(s_ph4);
+    __shared__ DevParams sp;
+    __shared__ int32_t sN[kMaxTileBursts];
+    __shared__ float sT[kMaxTileBursts];
+    __shared__ int32_t sOff[kMaxTileBursts + 1];
+    __shared__ unsigned int sh[kHistBins];
+    __shared__ int s_item;
+    __shared__ int s_staged;
+    const int tid = threadIdx.x;
+    int lim = 0;
+    for (;;) {
+        if (tid == 0) s_item = (int)atomicAdd(a.work, 1u);
+        __syncthreads();
+        const int item = s_item;
+        if (item >= a.n_items) break;
+        const int p = item / a.ntiles;
+        const int tile = item - p * a.ntiles;
+        const int64_t tb0 = a.b0 + (int64_t)tile * a.tile_b;
+        const int nb = (int)min((int64_t)a.tile_b, a.b1 - tb0);
+        {
+            const uint32_t *src = reinterpret_cast<const uint32_t *>(a.params + p);
+            uint32_t *dst = reinterpret_cast<uint32_t *>(&sp);
+            for (int i = tid; i < kParamWords; i += kThreads) dst[i] = src[i];
+        }
+        for (int i = tid; i < nb; i += kThreads) {
+            sN[i] = a.N[tb0 + i];
+            sT[i] = a.T[tb0 + i];
+        }
+        for (int i = tid; i < a.nbins; i += kThreads) sh[i] = 0u;
+        if (MODE == 1) {
+            // Stage the tile's offsets: copy the 16-byte-aligned span that
+            // covers [off_idx[tb0], off_idx[tb0+nb]) (the store is padded).
+            const int64_t first = a.off_idx[tb0];
+            const int64_t last = a.off_idx[tb0 + nb];
+            const int64_t abase = first & ~(int64_t)3;
+            const int64_t aend = (last + 3) & ~(int64_t)3;
+            const bool staged = (aend - abase) <= (int64_t)a.smem_cap;
+            if (staged) {
+                for (int i = tid; i <= nb; i += kThreads) sOff[i] = (int32_t)(a.off_idx[tb0 + i] - abase);
+                const float4 *src = reinterpret_cast<const float4 *>(a.offsets + abase);
+                const int nv = (int)((aend - abase) >> 2);
+                for (int i = tid; i < nv; i += kThreads) s_ph4[i] = __ldg(src + i);
+            }
+            if (tid == 0) s_staged = staged ? 1 : 0;
+        }
+        __syncthreads();
+        const int units = nb * a.S;
+        const bool staged = (MODE == 1) && s_staged;
+        for (int u = tid; u < units; u += kThreads) {
+            const int lb = u / a.S;
+            const int s = u - lb * a.S;
+            const int64_t b = tb0 + lb;
+            const int Nb = sN[lb];
+            const float Tb = sT[lb];
+            int A;
+            if (MODE == 0) {
+                A = unit_occ(sp, a.gamma, a.ct, a.r0, a.bg_a, a.bg_d, Nb, Tb, a.seed,
+                             a.pbase + (uint32_t)p, (uint32_t)b, (uint32_t)s, lim);
+            } else {
+                const float *offs = staged ? (s_ph + sOff[lb]) : (a.offsets + a.off_idx[b]);
+                A = unit_pho(sp, a.gamma, a.ct, a.r0, a.bg_a, a.bg_d, Nb, Tb, offs, a.seed,
+                             a.pbase + (uint32_t)p, (uint32_t)b, (uint32_t)s, lim);
+            }
+            if (a.unit_out) a.unit_out[((int64_t)p * (a.b1 - a.b0) + (b - a.b0)) * a.S + s] = A;
+            int bin = -1;
+            if (Nb > 0 && A >= 0) {
+                unsigned v = (unsigned)A * (unsigned)a.nbins / (unsigned)Nb;
+                bin = v >= (unsigned)a.nbins ? a.nbins - 1 : (int)v;
+            }
+            hist_add(sh, bin);
+        }
+        __syncthreads();
+        for (int i = tid; i < a.nbins; i += kThreads) {
+            unsigned v = sh[i];
+            if (v) atomicAdd(a.hist + (size_t)p * a.nbins + i, (unsigned long long)v);
+        }
+    }
+    if (lim) atomicAdd(a.limit_hits, (unsigned long long)lim);
+}
+
+__global__ void chi2_kernel(const unsigned long long *hist, const float *obs, int P, int nbins,
+                            int left_pad, int S, int n_states, double *chi2) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= P) return;
+    const unsigned long long *h = hist + (size_t)p * nbins;
+    int effN = nbins - left_pad;
+    double chi = 0.0;
+    for (int i = left_pad; i < nbins; ++i) {
+        if (h[i] > 0ull) {
+            double mi = (double)h[i] / (double)S;
+            double d = (double)obs[i] - mi;
+            chi = chi + d * d / mi;
+        } else {
+            effN -= 1;
+        }
+    }
+    chi2[p] = chi / (double)(effN - n_states * (n_states + 1));
+}
+
+// ---------------------------------------------------------------- ref-compat
+
+// drawDisIdx over n weights read through an index map (gen_rand.cuh:35-50)
+__device__ __forceinline__ int disidx_init(const float *p, int n, float pv) {
+    float acc = 0.0f;
+    for (int i = 0; i < n; ++i) {
+        acc = acc + p[i];
+        if (acc > pv) return i;
+    }
+    return n - 1;
+}
+
+// drawJ_Si2Sj (gen_rand.cuh:78-89): column si of P_i2j without the diagonal
+__device__ __forceinline__ int disidx_jump(const float *Pi2j, int n, int si, float pv) {
+    float acc = 0.0f;
+    const float *col = Pi2j + si * n;
+    int j = n - 2;
+    for (int ii = 0; ii < n - 1; ++ii) {
+        acc = acc + ((ii >= si) ? col[ii + 1] : col[ii]);
+        if (acc > pv) { j = ii; break; }
+    }
+    return (j >= si) ? j + 1 : j;
+}
+
+// saturating float->int64 truncation, NaN -> 0
+__device__ __forceinline__ int64_t f2i64(double v) {
+    if (v != v) return 0;
+    if (v >= 9.2233720368547758e18) return INT64_MAX;
+    if (v <= -9.2233720368547758e18) return INT64_MIN;
+    return (int64_t)v;
+}
+
+// draw_P_B_Tr (gen_rand.cuh:92-107) for one time bin
+__device__ __forceinline__ float bg_clip(Rng &r, float tot, float tdiff, float rate, int &lim) {
+    int sv = poisson(r, tdiff * rate, lim);
+    if ((float)sv <= tot) return (float)sv;
+    return floorf(tot * r.u01());
+}
+
+__global__ void __launch_bounds__(kThreads) rc_kernel(const RcArgs a) {
+    __shared__ DevParams sp;
+    __shared__ unsigned int sh[kHistBins];
+    const int tid = threadIdx.x;
+    {
+        const uint32_t *src = reinterpret_cast<const uint32_t *>(a.params);
+        uint32_t *dst = reinterpret_cast<uint32_t *>(&sp);
+        for (int i = tid; i < kParamWords; i += kThreads) dst[i] = src[i];
+    }
+    if (a.hist)
+        for (int i = tid; i < a.nbins; i += kThreads) sh[i] = 0u;
+    __syncthreads();
+    const int64_t NN = (int64_t)a.nb * a.R;
+    const int64_t tidx = (int64_t)blockIdx.x * kThreads + tid;
+    int lim = 0;
+    int bin = -1;
+    if (tidx < NN) {
+        const int lb = (int)(tidx / a.R);
+        const uint32_t s = (uint32_t)(tidx - (int64_t)lb * a.R);
+        const int64_t b = a.b0 + lb;
+        Rng r;
+        r.init(a.seed, a.pword, (uint32_t)b, s);
+        const int n = sp.n;
+        const int phCount = a.phCount[b];
+        const int64_t *bad = a.burst_ad + a.istart[b];
+        const int64_t *bdd = a.burst_dd + a.istart[b];
+        const float Tb = a.T[b];
+        const float clk = a.clk_p;
+        const float gam = a.gamma, dea = a.de, cht = a.ct, r0 = a.r0;
+        float F = 0.0f, mcE = 0.0f;
+        int si = disidx_init(sp.pinit, n, r.u01());
+        float spent = 0.0f;
+        int64_t bin0 = a.start[b], bin1 = a.start[b];
+        int binIdxStart = 0;
+        for (int seg = 0; Tb > spent && seg < kMaxSeg; ++seg) {
+            int sj = disidx_jump(sp.Pi2j, n, si, r.u01());
+            float st = logf_(r.u01()) / (-sp.K[si * n + sj]);
+            spent = spent + st;
+            if (spent >= Tb) bin1 = a.stop[b];
+            else bin1 = f2i64((double)((float)bin0 + spent / clk));
+            int sdd = 0, sad = 0, f_id = 0, f_ia = 0;
+            int ai = 0;
+            for (int iinb = binIdxStart; iinb < phCount; ++iinb) {
+                int64_t ddx = bdd[iinb], adx = bad[iinb];
+                if (ddx >= bin1 || adx >= bin1 || iinb == phCount - 1) {
+                    binIdxStart = iinb;
+                    float f_if = (gam - cht) * (float)f_id + (1.0f - dea) * (float)f_ia;
+                    float f_i;
+                    F = F + f_if;
+                    if ((double)a.bg_dd_rate < 1e-4) {
+                        f_i = floorf((float)((double)f_if + 0.5));
+                    } else {
+                        float tdiff = (float)(bin1 - bin0) * clk;
+                        float rf_ia = (1.0f - dea) * (float)f_ia;
+                        float bga = bg_clip(r, rf_ia, tdiff, a.bg_ad_rate, lim);
+                        float rf_id = (gam - cht) * (float)f_id;
+                        float bgd = bg_clip(r, rf_id, tdiff, a.bg_dd_rate, lim);
+                        f_i = floorf((float)((double)(f_if - bgd - bga) + 0.5));
+                    }
+                    float de = broaden(r, sp.E[si], r0, sp.V[si]);
+                    ai = binom(r, (int)f_i, de, lim);
+                    break;
+                }
+                if (ddx > 0) sdd = 1;
+                if (adx > 0) sad = 1;
+                if (sad && sdd) continue;
+                if (sad) f_ia++;
+                if (sdd) f_id++;
+            }
+            mcE = mcE + (float)ai;
+            bin0 = bin1;
+            si = sj;
+        }
+        if (F > 0.0f) mcE = mcE / F;
+        else mcE = 0.0f;
+        a.mcE[tidx] = mcE;
+        double z = (double)mcE;
+        if (z < 1.0 && z >= 0.0) bin = (int)(z * (double)a.nbins);
+    }
+    if (a.hist) {
+        if (tidx < NN) hist_add(sh, bin);
+        __syncthreads();
+        for (int i = tid; i < a.nbins; i += kThreads) {
+            unsigned v = sh[i];
+            if (v) atomicAdd(a.hist + i, (unsigned long long)v);
+        }
+    }
+    if (lim) atomicAdd(a.limit_hits, (unsigned long long)lim);
+}
+
+// ---------------------------------------------------------------- launchers
+
+cudaError_t launch_pda(int mode, const PdaArgs &a, int grid, size_t dyn_smem, cudaStream_t st) {
+    if (mode == 0) pda_kernel<0><<<grid, kThreads, dyn_smem, st>>>(a);
+    else pda_kernel<1><<<grid, kThreads, dyn_smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t pda_set_smem_limit(int mode, size_t dyn_smem) {
+    if (mode == 0) return cudaFuncSetAttribute(pda_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn_smem);
+    return cudaFuncSetAttribute(pda_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn_smem);
+}
+
+cudaError_t pda_occupancy_blocks(int mode, size_t dyn_smem, int *blocks_per_sm) {
+    if (mode == 0) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, pda_kernel<0>, kThreads, dyn_smem);
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, pda_kernel<1>, kThreads, dyn_smem);
+}
+
+cudaError_t launch_chi2(const unsigned long long *hist, const float *obs, int P, int nbins,
+                        int left_pad, int S, int n_states, double *chi2, cudaStream_t st) {
+    int threads = 128;
+    int grid = (P + threads - 1) / threads;
+    chi2_kernel<<<grid, threads, 0, st>>>(hist, obs, P, nbins, left_pad, S, n_states, chi2);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_rc(const RcArgs &a, cudaStream_t st) {
+    int64_t NN = (int64_t)a.nb * a.R;
+    if (NN <= 0) return cudaSuccess;
+    int64_t grid = (NN + kThreads - 1) / kThreads;
+    rc_kernel<<<(unsigned)grid, kThreads, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+}  // namespace gpda

@@ -1,0 +1,137 @@
+// gpda_params.cpp — host-side derivation of the per-parameter-set tables.
+//
+// Input: the reference's parameter vector (src/mc.cu:792-800)
+//   args = [E(n), K off-diagonals (n*n-n, row-major over i skipping i==j,
+//           K(i,j) = rate j->i), V(n)].
+// Output (DevParams):
+//   pda tables  — exit rates, 1/exit rates, cumulative jump probabilities per
+//                 source state, cumulative stationary distribution (solved in
+//                 FP64, K pi = 0, sum pi = 1), apparent acceptor probability
+//                 eps(E) = (g E + ct (1-E)) / (g E + (1+ct)(1-E)).
+//   rc tables   — genMatK (src/eigenhelper.cpp:4-22), genP_i2j (:24-38),
+//                 genMatP (:39-53) in the reference's float operation order.
+// All FP64 work is rounded once to FP32. Compiled with -ffp-contract=off.
+#include <cmath>
+#include <cstring>
+
+#include "gpda_internal.h"
+
+namespace gpda {
+
+namespace {
+
+inline float koff(const float *k, int n, int i, int j) {
+    return (i < j) ? k[i * (n - 1) + j - 1] : k[i * (n - 1) + j];
+}
+
+}  // namespace
+
+int build_params(int n, const float *args, float gamma, float ct, bool need_pi, DevParams *out) {
+    std::memset(out, 0, sizeof(*out));
+    if (n < 1 || n > 8 || args == nullptr) return -1;
+    const float *ko = args + n;
+    const float *V = args + n * n;
+    for (int i = 0; i < n; ++i) {
+        float e = args[i], v = V[i];
+        if (!(e >= 0.0f && e <= 1.0f)) return -1;
+        if (!(v >= 0.0f && v < INFINITY)) return -1;
+    }
+    double Kd[64];
+    double kexit[8];
+    double jcdf[64];
+    double kmax = 1.0;
+    for (int j = 0; j < n; ++j) {
+        double colsum = 0.0;
+        for (int i = 0; i < n; ++i) {
+            if (i == j) continue;
+            float k = koff(ko, n, i, j);
+            if (!(k >= 0.0f && k < INFINITY)) return -1;
+            Kd[j * n + i] = (double)k;
+            colsum += (double)k;
+            if ((double)k > kmax) kmax = (double)k;
+        }
+        Kd[j * n + j] = -colsum;
+        kexit[j] = colsum;
+        double acc = 0.0;
+        for (int i = 0; i < n; ++i) {
+            if (colsum > 0.0) {
+                if (i != j) acc += Kd[j * n + i];
+                jcdf[j * 8 + i] = acc / colsum;
+            } else {
+                jcdf[j * 8 + i] = 1.0;
+            }
+        }
+    }
+    double icdf[8];
+    if (need_pi) {
+        double A[8][9];
+        for (int i = 0; i < n; ++i) {
+            for (int j = 0; j < n; ++j) A[i][j] = Kd[j * n + i];
+            A[i][n] = 0.0;
+        }
+        for (int j = 0; j < n; ++j) A[n - 1][j] = 1.0;
+        A[n - 1][n] = 1.0;
+        for (int c = 0; c < n; ++c) {
+            int piv = c;
+            for (int r = c + 1; r < n; ++r)
+                if (std::fabs(A[r][c]) > std::fabs(A[piv][c])) piv = r;
+            if (!(std::fabs(A[piv][c]) > 1e-13 * kmax)) return -2;
+            if (piv != c)
+                for (int k = 0; k <= n; ++k) { double t = A[c][k]; A[c][k] = A[piv][k]; A[piv][k] = t; }
+            for (int r = c + 1; r < n; ++r) {
+                double f = A[r][c] / A[c][c];
+                for (int k = c; k <= n; ++k) A[r][k] = A[r][k] - f * A[c][k];
+            }
+        }
+        double pi[8];
+        for (int r = n - 1; r >= 0; --r) {
+            double s = A[r][n];
+            for (int k = r + 1; k < n; ++k) s = s - A[r][k] * pi[k];
+            pi[r] = s / A[r][r];
+        }
+        double sum = 0.0;
+        for (int i = 0; i < n; ++i) { if (!(pi[i] > 0.0)) pi[i] = 0.0; sum += pi[i]; }
+        if (!(sum > 0.0)) return -2;
+        double acc = 0.0;
+        for (int i = 0; i < n; ++i) { acc += pi[i] / sum; icdf[i] = acc; }
+    } else {
+        for (int i = 0; i < n; ++i) icdf[i] = (double)(i + 1) / (double)n;
+    }
+    out->n = n;
+    out->anyV = 0;
+    for (int i = 0; i < n; ++i) {
+        out->E[i] = args[i];
+        out->V[i] = V[i];
+        if (V[i] > 0.0f) out->anyV = 1;
+        out->kexit[i] = (float)kexit[i];
+        out->inv_kexit[i] = kexit[i] > 0.0 ? (float)(1.0 / kexit[i]) : INFINITY;
+        out->init_cdf[i] = (float)icdf[i];
+        float e = args[i];
+        float om = 1.0f - e;
+        float num = gamma * e + ct * om;
+        out->eps[i] = num / (num + om);
+        for (int j = 0; j < n; ++j) out->jump_cdf[i * 8 + j] = (float)jcdf[i * 8 + j];
+    }
+    // reference float tables (leading dimension n)
+    float *K = out->K, *P = out->Pi2j, *pinit = out->pinit;
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) K[i + j * n] = (i == j) ? 0.0f : koff(ko, n, i, j);
+    for (int j = 0; j < n; ++j)
+        for (int ii = 0; ii < n; ++ii)
+            if (ii != j) K[j + j * n] = K[j + j * n] - K[ii + j * n];
+    for (int j = 0; j < n; ++j) {
+        float sum = 0.0f;
+        for (int ii = 0; ii < n; ++ii)
+            if (ii != j) sum = sum + K[ii + j * n];
+        for (int ii = 0; ii < n; ++ii) P[ii + j * n] = (ii != j) ? K[ii + j * n] / sum : 0.0f;
+    }
+    for (int i = 0; i < n; ++i) {
+        float s = 0.0f;
+        for (int j = 0; j < n; ++j) s = s + K[i + j * n];
+        s = s - K[i + i * n];
+        pinit[i] = s;
+    }
+    return 0;
+}
+
+}  // namespace gpda

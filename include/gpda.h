@@ -1,0 +1,205 @@
+/*
+ * gpda.h — C ABI of the GB300-native photon-burst Monte-Carlo PDA engine.
+ *
+ * Plain pointers and sizes only; every entry point returns an int status
+ * (GPDA_OK = 0, negative on error) and never exits the process. A context is
+ * bound to one device and driven by one host thread at a time.
+ *
+ * Two families of entry points:
+ *
+ *   gpda_mc_*  — the drop-in for the reference's `mc` engine object
+ *                (src/mc.hpp:32-180, src/mc.cu:212-829). Same call sequence
+ *                as gpuWorker::run (src/gpuWorker.cpp:69-82), same argument
+ *                meaning and parameter layout; kernel semantics are mc_kernel's
+ *                (src/mc.cu:83-197) with Philox counters instead of per-thread
+ *                Sobol/xorshift states. include/gpda_mc.hpp wraps them in a C++
+ *                class with the reference's member names.
+ *
+ *   gpda_*     — the physical PDA model (occupancy-weighted E, or photon-by-
+ *                photon state assignment), fused on device with the
+ *                proximity-ratio histogram and the reduced chi-square that
+ *                streamWorker::run computes on the host
+ *                (src/streamWorker.cpp:184-206).
+ *
+ * Parameter vectors use the reference layout (src/mc.cu:792-800):
+ *   [E(n), K off-diagonals (n*n-n, row-major skipping the diagonal,
+ *    K(i,j) = rate j->i as in genMatK, src/eigenhelper.cpp:4-22), V(n)].
+ */
+#ifndef GPDA_H
+#define GPDA_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GPDA_MAX_STATES 8
+#define GPDA_MAX_BINS 1024
+
+enum {
+    GPDA_OK = 0,
+    GPDA_ERR_ARG = -1,       /* invalid argument (sizes, ranges, NULL, unsorted offsets) */
+    GPDA_ERR_SINGULAR = -2,  /* rate matrix has no unique stationary distribution */
+    GPDA_ERR_CUDA = -3,      /* CUDA runtime error (message in gpda_last_error) */
+    GPDA_ERR_NOMEM = -4,     /* device or pinned host allocation failed */
+    GPDA_ERR_STATE = -5,     /* call out of order (e.g. run before upload) */
+    GPDA_ERR_LIMIT = -6      /* a bounded device loop hit its limit (counted, see gpda_limit_hits) */
+};
+
+enum { GPDA_MODE_OCCUPANCY = 0, GPDA_MODE_PHOTON = 1 };
+
+/* Model constants. Defaults: nbins 21, left_pad 2, gamma 1, crosstalk 0.05,
+ * bg_d 1500/s, bg_a 800/s, r0 52; ref-compat constants are mc_kernel's
+ * defaults gamma 0.34, DexDirAem 0.08, Dch2Ach 0.07, r0 52 (src/mc.cu:89-91). */
+typedef struct {
+    int32_t nbins;      /* histogram bins on [0,1] (<= GPDA_MAX_BINS) */
+    int32_t left_pad;   /* first bin counted in the chi-square (main.cpp:155 passes 2) */
+    float gamma;        /* detection-efficiency ratio */
+    float crosstalk;    /* donor->acceptor leakage */
+    float bg_d;         /* donor-channel background rate (1/s) */
+    float bg_a;         /* acceptor-channel background rate (1/s) */
+    float r0;           /* Foerster radius for distance broadening (V > 0) */
+    float rc_gamma;
+    float rc_de;
+    float rc_ct;
+    float rc_r0;
+} gpda_model;
+
+typedef struct gpda_ctx gpda_ctx;
+
+/* Fill *m with the defaults above. */
+void gpda_model_defaults(gpda_model *m);
+
+/* Library version string. */
+const char *gpda_version(void);
+
+/* ---------------------------------------------------------------- pda */
+
+/* Create a context on `device`. Replaces mc::mc (src/mc.cu:212-315): no RNG
+ * state tables, no stream pool; one CUDA stream owned by the context. */
+gpda_ctx *gpda_create(int32_t device, const gpda_model *m, int32_t *status);
+void gpda_destroy(gpda_ctx *ctx);
+/* Message of the last failed call on this context ("" if none). */
+const char *gpda_last_error(const gpda_ctx *ctx);
+
+/* Copy a burst set from host memory into HBM. Replaces mc::init_data_gpu
+ * (src/mc.cu:456-521) for the pda model: N int32[B] photons per burst,
+ * T float[B] durations (s), and for photon mode off_idx int64[B+1] prefix
+ * offsets into offsets float[off_idx[B]] (sorted arrival offsets in [0,T],
+ * seconds; checked). off_idx/offsets may be NULL for occupancy mode. */
+int32_t gpda_upload_bursts(gpda_ctx *ctx, const int32_t *N, const float *T,
+                           const int64_t *off_idx, const float *offsets, int64_t B);
+
+/* Observed histogram (nbins floats) used by the chi-square. Replaces the
+ * per-thread mkhist of SgDivSr in streamWorker::run (src/streamWorker.cpp:62-67). */
+int32_t gpda_set_observed(gpda_ctx *ctx, const float *ohist, int32_t nbins);
+
+/* Bin observed proximity ratios with the reference's rule (Boost regular axis
+ * on [0,1), inner bins only, src/streamWorker.cpp:33-38). Host-only helper. */
+int32_t gpda_bin_values(const float *x, int64_t n, int32_t nbins, float *hist_out);
+
+/* Derive the per-parameter-set tables the kernels use (stationary
+ * distribution, jump CDFs, exit rates, apparent efficiencies) into a
+ * caller buffer of gpda_params_size() floats. Host-only; exposed for tests.
+ * Replaces genMatK/genP_i2j/genMatP (src/eigenhelper.cpp:4-53). */
+int32_t gpda_params_size(void);
+int32_t gpda_build_params(const gpda_model *m, int32_t n_states, const float *args, float *out);
+
+/* One parameter set over bursts [b0,b1), `samples` MC draws per burst:
+ * launch + fused histogram (+ chi-square if an observed histogram is set),
+ * synchronous. hist_out: nbins uint64 counts (nullable); chi2_out (nullable).
+ * Replaces set_params + run_kernel + the host histogram/chi-square
+ * (src/mc.cu:567-587, src/streamWorker.cpp:184-206). */
+int32_t gpda_run_plain(gpda_ctx *ctx, int32_t mode, int32_t n_states, const float *params,
+                       int64_t b0, int64_t b1, int32_t samples, uint64_t seed,
+                       uint64_t *hist_out, double *chi2_out);
+
+/* A population of P parameter sets over all bursts in one persistent launch
+ * (graph-captured). params: P*n(n+1) floats. hist_out: P*nbins (nullable),
+ * chi2_out: P (nullable). Synchronous. */
+int32_t gpda_run_batched(gpda_ctx *ctx, int32_t mode, int32_t P, int32_t n_states,
+                         const float *params, int32_t samples, uint64_t seed,
+                         uint64_t *hist_out, double *chi2_out);
+
+/* Per-unit acceptor counts for parity checking: unit_out int32[P][b1-b0][samples]
+ * (host), -1 where N == 0. Same random counters as the runs above. */
+int32_t gpda_run_units(gpda_ctx *ctx, int32_t mode, int32_t P, int32_t n_states,
+                       const float *params, int64_t b0, int64_t b1, int32_t samples,
+                       uint64_t seed, int32_t *unit_out, uint64_t *hist_out);
+
+/* Asynchronous form for resident-data measurement: parameters are staged
+ * through pinned memory, results stay on the device until gpda_fetch. */
+int32_t gpda_launch(gpda_ctx *ctx, int32_t mode, int32_t P, int32_t n_states,
+                    const float *params, int64_t b0, int64_t b1, int32_t samples,
+                    uint64_t seed);
+int32_t gpda_fetch(gpda_ctx *ctx, uint64_t *hist_out, double *chi2_out);
+/* Non-blocking completion check, like mc::streamQuery (src/mc.cu:595-601):
+ * 1 = done, 0 = pending, <0 = error. */
+int32_t gpda_query(gpda_ctx *ctx);
+int32_t gpda_synchronize(gpda_ctx *ctx);
+/* The context's CUDA stream (a cudaStream_t), for event timing by callers. */
+void *gpda_stream(gpda_ctx *ctx);
+/* Kernel launches issued so far on this context. */
+int64_t gpda_launch_count(const gpda_ctx *ctx);
+/* Number of units whose segment/rejection loops hit their bound so far. */
+int64_t gpda_limit_hits(gpda_ctx *ctx);
+
+/* ---------------------------------------------------------------- mc drop-in */
+
+typedef struct gpda_mc gpda_mc;
+
+/* mc::mc(devid, streamNum, debug, hdf5size, profiler) (src/mc.cu:212).
+ * streamNum 0 picks 2 x asyncEngineCount as the reference does (mc.cu:61-66). */
+gpda_mc *gpda_mc_create(int32_t devid, int32_t streamNum, uint8_t debug, uint64_t hdf5size,
+                        int32_t profiler, int32_t *status);
+void gpda_mc_destroy(gpda_mc *mc);
+const char *gpda_mc_last_error(const gpda_mc *mc);
+int32_t gpda_mc_stream_num(const gpda_mc *mc);            /* mc::getStreams (mc.cu:317) */
+int32_t gpda_mc_sz_burst(const gpda_mc *mc);              /* mc::sz_burst */
+int32_t gpda_mc_resample_times(const gpda_mc *mc);        /* mc::reSampleTimes (mc.hpp:87) */
+/* mc::set_reSampleTimes (mc.cu:316); any value >= 1 is accepted (the
+ * reference rounds down to a power of two because of its index shift). */
+int32_t gpda_mc_set_resample_times(gpda_mc *mc, int32_t r);
+/* Seed of the Philox key (the reference seeds curand with offset 1234). */
+int32_t gpda_mc_set_seed(gpda_mc *mc, uint64_t seed);
+/* Model constants of the ref-compat kernel (default: mc_kernel's). */
+int32_t gpda_mc_set_model(gpda_mc *mc, const gpda_model *m);
+
+/* mc::init_data_gpu (mc.cu:456-521): host arrays copied into HBM. */
+int32_t gpda_mc_init_data_gpu(gpda_mc *mc, const int64_t *istart, const int64_t *start,
+                              const int64_t *stop, const int32_t *phCount, int64_t n_bursts,
+                              int64_t sz_tag, const int64_t *burst_ad, const int64_t *burst_dd,
+                              const float *T_burst_duration, const float *SgDivSr,
+                              float clk_p, float bg_ad_rate, float bg_dd_rate);
+/* mc::set_nstates (mc.cu:723-781): returns the previous n of stream sid. */
+int32_t gpda_mc_set_nstates(gpda_mc *mc, int32_t n, int32_t sid);
+/* mc::set_params (mc.cu:790-829): 1 on success, 0 if nargs != n(n+1)
+ * (the reference's genMatK size check, eigenhelper.cpp:5-8), <0 on error. */
+int32_t gpda_mc_set_params(gpda_mc *mc, int32_t n, int32_t sid, const float *args, int32_t nargs);
+/* mc::setBurstBd (mc.cu:523-565): returns N bursts of the range. */
+int32_t gpda_mc_setBurstBd(gpda_mc *mc, int32_t cstart, int32_t cstop, int32_t sid);
+/* mc::init_randstate (mc.cu:366-454): counter-based RNG needs no state
+ * tables; records N. */
+int32_t gpda_mc_init_randstate(gpda_mc *mc, int32_t N, int32_t sid);
+/* mc::set_params_buff (mc.cu:783-788): the per-thread P_i2j scratch lives in
+ * registers here; kept for the call sequence. */
+int32_t gpda_mc_set_params_buff(gpda_mc *mc, int32_t oldS_n, int32_t N, int32_t sid);
+/* mc::run_kernel (mc.cu:567-587): async launch of the ref-compat kernel on
+ * stream sid and async copy of N*reSampleTimes floats into hmcE(sid); also
+ * bins the values on device into the stream's histogram. */
+int32_t gpda_mc_run_kernel(gpda_mc *mc, int32_t N, int32_t sid);
+/* mc::streamQuery (mc.cu:595-601): 1 done, 0 pending. */
+int32_t gpda_mc_streamQuery(gpda_mc *mc, int32_t sid);
+/* mc::hmcE[sid] (mc.hpp:83): pinned host results of the last run_kernel. */
+float *gpda_mc_hmcE(gpda_mc *mc, int32_t sid);
+/* Histogram bins used by the fused on-device histogram (fretHistNum, -f). */
+int32_t gpda_mc_set_hist_bins(gpda_mc *mc, int32_t nbins);
+/* Device-binned histogram of the last completed run on stream sid (nbins
+ * floats, reference binning rule). Call after streamQuery returned 1. */
+int32_t gpda_mc_hist(gpda_mc *mc, int32_t sid, float *hist_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

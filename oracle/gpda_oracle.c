@@ -1,0 +1,531 @@
+/*
+ * gpda_oracle.c — CPU oracle for the photon-burst Monte-Carlo PDA path.
+ *
+ * TEST INFRASTRUCTURE ONLY (the checker, never the product). See
+ * gpda_oracle.h for what is restated and which reference lines it follows.
+ *
+ * Build: gcc -O3 -fopenmp -ffp-contract=off -fno-fast-math -shared -fPIC
+ * (oracle/build_oracle.py). -ffp-contract=off is required: every FP32
+ * operation must round exactly where the device code rounds.
+ */
+#include "gpda_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* ------------------------------------------------------------------ */
+/* Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as
+ * easy as 1, 2, 3", SC'11): multipliers and Weyl key increments from the
+ * paper; 10 rounds, key bumped between rounds. */
+#define PHX_M0 0xD2511F53u
+#define PHX_M1 0xCD9E8D57u
+#define PHX_W0 0x9E3779B9u
+#define PHX_W1 0xBB67AE85u
+
+void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
+    uint32_t c0 = ctr[0], c1 = ctr[1], c2 = ctr[2], c3 = ctr[3];
+    uint32_t k0 = key[0], k1 = key[1];
+    for (int r = 0; r < 10; ++r) {
+        uint64_t p0 = (uint64_t)PHX_M0 * c0;
+        uint64_t p1 = (uint64_t)PHX_M1 * c2;
+        uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+        uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+        uint32_t n0 = hi1 ^ c1 ^ k0;
+        uint32_t n2 = hi0 ^ c3 ^ k1;
+        c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+        k0 += PHX_W0; k1 += PHX_W1;
+    }
+    out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+/* One unit's draw stream: counter (block, sample, burst, param-set word). */
+typedef struct {
+    uint32_t key[2];
+    uint32_t ctr[4];
+    uint32_t buf[4];
+    int idx;
+} orc_rng;
+
+static inline void rng_init(orc_rng *r, uint64_t seed, uint32_t pword, uint32_t b, uint32_t s) {
+    r->key[0] = (uint32_t)seed;
+    r->key[1] = (uint32_t)(seed >> 32);
+    r->ctr[0] = 0; r->ctr[1] = s; r->ctr[2] = b; r->ctr[3] = pword;
+    r->idx = 4;
+}
+static inline uint32_t rng_next(orc_rng *r) {
+    if (r->idx == 4) {
+        orc_philox4x32_10(r->ctr, r->key, r->buf);
+        r->ctr[0] += 1u;
+        r->idx = 0;
+    }
+    return r->buf[r->idx++];
+}
+
+/* ------------------------------------------------------------------ */
+/* FP32 elementary functions, written from the mathematics (no libm, no
+ * vendor code): identical operation order on the device makes them
+ * bit-reproducible. Constants are float(1/k) etc., given in hex. */
+static inline float f_from_bits(uint32_t u) { float f; memcpy(&f, &u, 4); return f; }
+static inline uint32_t bits_from_f(float f) { uint32_t u; memcpy(&u, &f, 4); return u; }
+
+#define C_LN2_HI 0x1.62e430p-1f     /* float(ln 2) */
+#define C_LN2_LO -0x1.05c610p-29f   /* ln 2 - C_LN2_HI */
+#define C_LOG2E 0x1.715476p+0f
+#define C_SQRT2 0x1.6a09e6p+0f
+
+/* log(x): x = 2^e m, m in [sqrt(2)/2, sqrt(2)); log m = 2 atanh(s),
+ * s = (m-1)/(m+1), atanh series to s^9. */
+float orc_logf(float x) {
+    if (x != x) return x;
+    if (x < 0.0f) return NAN;
+    if (x == 0.0f) return -INFINITY;
+    if (x == INFINITY) return x;
+    uint32_t bits = bits_from_f(x);
+    int e = 0;
+    if ((bits >> 23) == 0u) {           /* subnormal: scale by 2^24 */
+        x = x * 0x1p24f;
+        bits = bits_from_f(x);
+        e = -24;
+    }
+    e += (int)(bits >> 23) - 127;
+    float m = f_from_bits((bits & 0x007FFFFFu) | 0x3F800000u);
+    if (m > C_SQRT2) { m = m * 0.5f; e += 1; }
+    float f = m - 1.0f;
+    float s = f / (2.0f + f);
+    float z = s * s;
+    float poly = fmaf(z, fmaf(z, fmaf(z, 0x1.c71c72p-3f, 0x1.24924ap-2f), 0x1.99999ap-2f), 0x1.555556p-1f);
+    float lm = fmaf(s * z, poly, 2.0f * s);
+    float ef = (float)e;
+    return fmaf(ef, C_LN2_HI, fmaf(ef, C_LN2_LO, lm));
+}
+
+/* exp(x): x = k ln2 + r, |r| <= ln2/2, Taylor series of e^r to r^7. */
+float orc_expf(float x) {
+    if (x != x) return x;
+    if (x > 88.72284f) return INFINITY;
+    if (x < -103.97208f) return 0.0f;
+    float kf = rintf(x * C_LOG2E);
+    float r = fmaf(-kf, C_LN2_HI, x);
+    r = fmaf(-kf, C_LN2_LO, r);
+    float p = 0x1.a01a02p-13f;
+    p = fmaf(p, r, 0x1.6c16c2p-10f);
+    p = fmaf(p, r, 0x1.111112p-7f);
+    p = fmaf(p, r, 0x1.555556p-5f);
+    p = fmaf(p, r, 0x1.555556p-3f);
+    p = fmaf(p, r, 0.5f);
+    p = fmaf(p, r, 1.0f);
+    p = fmaf(p, r, 1.0f);
+    int k = (int)kf;
+    if (k >= -126 && k <= 127) return p * f_from_bits((uint32_t)(k + 127) << 23);
+    int k1 = k / 2, k2 = k - k1;
+    return (p * f_from_bits((uint32_t)(k1 + 127) << 23)) * f_from_bits((uint32_t)(k2 + 127) << 23);
+}
+
+/* cos(2 pi u) for u in [0,1]: fold to w in [0,1/2], cos(2 pi w) = sin(2 pi (1/4 - w)),
+ * sine Taylor series to theta^13. */
+float orc_cos2pif(float u) {
+    float w = (u > 0.5f) ? 1.0f - u : u;
+    float rr = 0.25f - w;
+    float th = rr * 0x1.921fb6p+2f;
+    float t2 = th * th;
+    float p = 0x1.612462p-33f;
+    p = fmaf(p, t2, -0x1.ae6456p-26f);
+    p = fmaf(p, t2, 0x1.71de3ap-19f);
+    p = fmaf(p, t2, -0x1.a01a02p-13f);
+    p = fmaf(p, t2, 0x1.111112p-7f);
+    p = fmaf(p, t2, -0x1.555556p-3f);
+    p = fmaf(p, t2, 1.0f);
+    return th * p;
+}
+
+/* Stirling correction fc(k) = ln k! - ((k+1/2) ln(k+1) - (k+1) + ln(2 pi)/2),
+ * k = 0..9, from lgamma in double (Hoermann 1993, BTRD). */
+static const float FC_TAB[10] = {
+    8.106146680e-02f, 4.134069596e-02f, 2.767792568e-02f, 2.079067210e-02f,
+    1.664469119e-02f, 1.387612882e-02f, 1.189670995e-02f, 1.041126526e-02f,
+    9.255462183e-03f, 8.330563433e-03f};
+/* ln k!, k = 0..9 */
+static const float LF_TAB[10] = {
+    0.0f, 0.0f, 0.693147182f, 1.791759491f, 3.178053856f,
+    4.787491798f, 6.579251289f, 8.525161743f, 10.60460281f, 12.80182743f};
+static const double FC_TAB_D[10] = {
+    0.08106146679532733, 0.04134069595540946, 0.027677925684997717, 0.02079067210376584,
+    0.01664469118982126, 0.013876128823072875, 0.011896709945893313, 0.010411265261973668,
+    0.00925546218270945, 0.008330563433359472};
+
+/* saturating float->int64 truncation with NaN -> 0 (PTX cvt.rzi.s64 semantics) */
+static inline int64_t f2i64(double v) {
+    if (v != v) return 0;
+    if (v >= 9.2233720368547758e18) return INT64_MAX;
+    if (v <= -9.2233720368547758e18) return INT64_MIN;
+    return (int64_t)v;
+}
+
+/* ------------------------------------------------------------------ */
+/* Host parameter derivation in double (the product derives the same way). */
+typedef struct {
+    int n;
+    double E[ORC_MAXS], V[ORC_MAXS];
+    double Kd[ORC_MAXS * ORC_MAXS];   /* column-major with leading dim n, diag = -column sum */
+    double kexit[ORC_MAXS];
+    double jump_cdf[ORC_MAXS * ORC_MAXS];
+    double init_cdf[ORC_MAXS];
+} orc_derived;
+
+/* K(i,j) (rate j->i) from the reference's off-diagonal layout
+ * (eigenhelper.cpp:4-22): i<j -> args[i*(n-1)+j-1], i>j -> args[i*(n-1)+j]. */
+static inline float koff_at(const float *koff, int n, int i, int j) {
+    return (i < j) ? koff[i * (n - 1) + j - 1] : koff[i * (n - 1) + j];
+}
+
+static int derive_double(int n, const float *args, orc_derived *d, int need_pi) {
+    if (n < 1 || n > ORC_MAXS) return -1;
+    const float *koff = args + n;
+    const float *V = args + n * n;
+    d->n = n;
+    double kmax = 1.0;
+    for (int i = 0; i < n; ++i) {
+        float e = args[i], v = V[i];
+        if (!(e >= 0.0f && e <= 1.0f)) return -1;
+        if (!(v >= 0.0f && v < INFINITY)) return -1;
+        d->E[i] = e; d->V[i] = v;
+    }
+    for (int j = 0; j < n; ++j) {
+        double colsum = 0.0;
+        for (int i = 0; i < n; ++i) {
+            if (i == j) continue;
+            float k = koff_at(koff, n, i, j);
+            if (!(k >= 0.0f && k < INFINITY)) return -1;
+            d->Kd[j * n + i] = (double)k;
+            colsum += (double)k;
+            if ((double)k > kmax) kmax = (double)k;
+        }
+        d->Kd[j * n + j] = -colsum;
+        d->kexit[j] = colsum;
+        double acc = 0.0;
+        for (int i = 0; i < n; ++i) {
+            if (colsum > 0.0) {
+                if (i != j) acc += d->Kd[j * n + i];
+                d->jump_cdf[j * ORC_MAXS + i] = acc / colsum;
+            } else {
+                d->jump_cdf[j * ORC_MAXS + i] = 1.0;
+            }
+        }
+    }
+    if (!need_pi) {
+        for (int i = 0; i < n; ++i) d->init_cdf[i] = (double)(i + 1) / (double)n;
+        return 0;
+    }
+    /* stationary distribution: K pi = 0 with the last equation replaced by
+     * sum(pi) = 1, Gaussian elimination with partial pivoting. */
+    double A[ORC_MAXS][ORC_MAXS + 1];
+    for (int i = 0; i < n; ++i) {
+        for (int j = 0; j < n; ++j) A[i][j] = d->Kd[j * n + i];
+        A[i][n] = 0.0;
+    }
+    for (int j = 0; j < n; ++j) A[n - 1][j] = 1.0;
+    A[n - 1][n] = 1.0;
+    for (int c = 0; c < n; ++c) {
+        int piv = c;
+        for (int r = c + 1; r < n; ++r)
+            if (fabs(A[r][c]) > fabs(A[piv][c])) piv = r;
+        if (!(fabs(A[piv][c]) > 1e-13 * kmax)) return -2;
+        if (piv != c)
+            for (int k = 0; k <= n; ++k) { double t = A[c][k]; A[c][k] = A[piv][k]; A[piv][k] = t; }
+        for (int r = c + 1; r < n; ++r) {
+            double f = A[r][c] / A[c][c];
+            for (int k = c; k <= n; ++k) A[r][k] = A[r][k] - f * A[c][k];
+        }
+    }
+    double pi[ORC_MAXS];
+    for (int r = n - 1; r >= 0; --r) {
+        double s = A[r][n];
+        for (int k = r + 1; k < n; ++k) s = s - A[r][k] * pi[k];
+        pi[r] = s / A[r][r];
+    }
+    double sum = 0.0;
+    for (int i = 0; i < n; ++i) { if (!(pi[i] > 0.0)) pi[i] = 0.0; sum += pi[i]; }
+    if (!(sum > 0.0)) return -2;
+    double acc = 0.0;
+    for (int i = 0; i < n; ++i) { acc += pi[i] / sum; d->init_cdf[i] = acc; }
+    return 0;
+}
+
+/* Reference float tables, in the reference's operation order:
+ * genMatK (eigenhelper.cpp:4-22), genP_i2j (:24-38), genMatP (:39-53). */
+static void ref_tables_f(int n, const float *args, float *K, float *P, float *pinit) {
+    const float *koff = args + n;
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j)
+            K[i + j * n] = (i == j) ? 0.0f : koff_at(koff, n, i, j);
+    for (int j = 0; j < n; ++j)
+        for (int ii = 0; ii < n; ++ii)
+            if (ii != j) K[j + j * n] = K[j + j * n] - K[ii + j * n];
+    for (int j = 0; j < n; ++j) {
+        float sum = 0.0f;
+        for (int ii = 0; ii < n; ++ii) if (ii != j) sum = sum + K[ii + j * n];
+        for (int ii = 0; ii < n; ++ii)
+            P[ii + j * n] = (ii != j) ? K[ii + j * n] / sum : 0.0f;
+    }
+    for (int i = 0; i < n; ++i) {
+        float s = 0.0f;
+        for (int j = 0; j < n; ++j) s = s + K[i + j * n];
+        s = s - K[i + i * n];
+        pinit[i] = s;
+    }
+}
+static void ref_tables_d(int n, const float *args, double *K, double *P, double *pinit) {
+    const float *koff = args + n;
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j)
+            K[i + j * n] = (i == j) ? 0.0 : (double)koff_at(koff, n, i, j);
+    for (int j = 0; j < n; ++j)
+        for (int ii = 0; ii < n; ++ii)
+            if (ii != j) K[j + j * n] = K[j + j * n] - K[ii + j * n];
+    for (int j = 0; j < n; ++j) {
+        double sum = 0.0;
+        for (int ii = 0; ii < n; ++ii) if (ii != j) sum = sum + K[ii + j * n];
+        for (int ii = 0; ii < n; ++ii)
+            P[ii + j * n] = (ii != j) ? K[ii + j * n] / sum : 0.0;
+    }
+    for (int i = 0; i < n; ++i) {
+        double s = 0.0;
+        for (int j = 0; j < n; ++j) s = s + K[i + j * n];
+        s = s - K[i + i * n];
+        pinit[i] = s;
+    }
+}
+
+static inline int pda_bin(int A, int N, int nbins) {
+    if (N <= 0 || A < 0) return -1;
+    long long v = (long long)A * nbins / N;
+    if (v >= nbins) v = nbins - 1;
+    return (int)v;
+}
+
+/* Boost.Histogram regular axis on [0,1): z in double; inner bins only. */
+static inline int ref_bin_d(double z, int nbins) {
+    if (z < 1.0) {
+        if (z >= 0.0) return (int)(z * (double)nbins);
+        return -1;
+    }
+    return -1;
+}
+
+#define ORC_MAX_SEG 65536
+#define ORC_MAX_RESTART 256
+
+/* ------------------------------------------------------------------ */
+/* FP32 instantiation: bit-exact mirror of the device kernels. */
+#define REAL float
+#define RL(x) x##f
+#define LOGR orc_logf
+#define EXPR orc_expf
+#define SQRTR sqrtf
+#define FLOORR floorf
+#define FABSR fabsf
+#define FMAR fmaf
+#define COS2PIR orc_cos2pif
+#define COPYSIGNR copysignf
+#define INFR INFINITY
+#define FC_T FC_TAB
+#define LF_T LF_TAB
+#define PFX(x) f32_##x
+#include "gpda_oracle_core.inc"
+#undef REAL
+#undef RL
+#undef LOGR
+#undef EXPR
+#undef SQRTR
+#undef FLOORR
+#undef FABSR
+#undef FMAR
+#undef COS2PIR
+#undef COPYSIGNR
+#undef INFR
+#undef FC_T
+#undef LF_T
+#undef PFX
+
+/* FP64 transcription on the same counters. */
+static double lf_tab_d[10];
+static double cos2pi_d(double u) { return cos(6.283185307179586 * u); }
+#define REAL double
+#define RL(x) x
+#define LOGR log
+#define EXPR exp
+#define SQRTR sqrt
+#define FLOORR floor
+#define FABSR fabs
+#define FMAR fma
+#define COS2PIR cos2pi_d
+#define COPYSIGNR copysign
+#define INFR ((double)INFINITY)
+#define FC_T FC_TAB_D
+#define LF_T lf_tab_d
+#define PFX(x) f64_##x
+#include "gpda_oracle_core.inc"
+
+static void init_lf_d(void) {
+    static int done = 0;
+    if (done) return;
+    for (int k = 0; k < 10; ++k) lf_tab_d[k] = lgamma((double)k + 1.0);
+    done = 1;
+}
+
+/* ------------------------------------------------------------------ */
+int orc_build_params(int32_t n, const float *args, const orc_model *m, orc_params *out) {
+    (void)m;
+    orc_derived d;
+    memset(out, 0, sizeof(*out));
+    int rc = derive_double(n, args, &d, 1);
+    if (rc != 0) return rc;
+    out->n = n;
+    for (int i = 0; i < n; ++i) {
+        out->E[i] = args[i];
+        out->V[i] = args[n * n + i];
+        out->kexit[i] = (float)d.kexit[i];
+        out->inv_kexit[i] = d.kexit[i] > 0.0 ? (float)(1.0 / d.kexit[i]) : INFINITY;
+        out->init_cdf[i] = (float)d.init_cdf[i];
+        float e = args[i];
+        float om = 1.0f - e;
+        float num = m->gamma * e + m->crosstalk * om;
+        out->eps[i] = num / (num + om);
+        for (int j = 0; j < n; ++j) out->jump_cdf[i * ORC_MAXS + j] = (float)d.jump_cdf[i * ORC_MAXS + j];
+    }
+    ref_tables_f(n, args, out->K, out->Pi2j, out->pinit);
+    return 0;
+}
+
+int orc_sample(int kind, uint64_t seed, int32_t n, float p, int64_t count, double *out) {
+    init_lf_d();
+    for (int64_t i = 0; i < count; ++i) {
+        orc_rng r;
+        rng_init(&r, seed, 0u, 0u, (uint32_t)i);
+        switch (kind) {
+        case 0: out[i] = (double)f32_binom(&r, n, p); break;
+        case 1: out[i] = (double)f32_poisson(&r, p); break;
+        case 2: out[i] = (double)(-orc_logf(f32_u01(&r)) * (1.0f / p)); break;
+        case 3: out[i] = (double)f32_normal(&r); break;
+        case 4: out[i] = (double)f32_u01(&r); break;
+        case 5: out[i] = (double)f64_binom(&r, n, (double)p); break;
+        case 6: out[i] = (double)f64_poisson(&r, (double)p); break;
+        default: return -1;
+        }
+    }
+    return 0;
+}
+
+/* categorical draws: mode 0 pda initial-state draw over a cumulative table
+ * w[n]; mode 1 drawDisIdx over unnormalised weights w[n] (gen_rand.cuh:35-50);
+ * mode 2 pda jump draw from `from` over the cumulative row w[n]; mode 3
+ * drawJ_Si2Sj from `from` over the column-major n x n matrix w (:78-89). */
+int orc_sample_cat(uint64_t seed, int32_t mode, int32_t n, const float *w, int32_t from,
+                   int64_t count, int32_t *out) {
+    if (n < 1 || n > ORC_MAXS || !w || !out || from < 0 || from >= n) return -1;
+    for (int64_t i = 0; i < count; ++i) {
+        orc_rng r;
+        rng_init(&r, seed, 0u, 0u, (uint32_t)i);
+        float u = f32_u01(&r);
+        switch (mode) {
+        case 0: out[i] = f32_cat(w, n, u); break;
+        case 1: out[i] = f32_disidx(n, w, u); break;
+        case 2: out[i] = f32_jump(w, n, from, u); break;
+        case 3: {
+            float col[ORC_MAXS];
+            for (int ii = 0; ii < n - 1; ++ii)
+                col[ii] = (ii >= from) ? w[from * n + ii + 1] : w[from * n + ii];
+            int j = f32_disidx(n - 1, col, u);
+            out[i] = (j >= from) ? j + 1 : j;
+            break;
+        }
+        default: return -1;
+        }
+    }
+    return 0;
+}
+
+static int check_model(const orc_model *m) {
+    if (m->nbins < 1 || m->nbins > 4096) return -1;
+    if (m->left_pad < 0 || m->left_pad > m->nbins) return -1;
+    if (!(m->gamma > 0.0f && m->gamma < INFINITY)) return -1;
+    if (!(m->crosstalk >= 0.0f && m->crosstalk < INFINITY)) return -1;
+    if (!(m->bg_d >= 0.0f && m->bg_d < INFINITY)) return -1;
+    if (!(m->bg_a >= 0.0f && m->bg_a < INFINITY)) return -1;
+    if (!(m->r0 > 0.0f && m->rc_r0 > 0.0f)) return -1;
+    return 0;
+}
+
+int orc_run_pda(const orc_bursts *bs, int32_t n, const float *args, int32_t P,
+                const orc_model *m, int32_t mode, int32_t S, uint64_t seed,
+                int64_t b0, int64_t b1, uint64_t *hist, int32_t *unit_out,
+                int32_t nthreads, int32_t f64) {
+    if (!bs || !args || !m || !hist) return -1;
+    if (P < 1 || S < 1 || b0 < 0 || b1 < b0 || b1 > bs->B) return -1;
+    if (mode != ORC_MODE_OCCUPANCY && mode != ORC_MODE_PHOTON) return -1;
+    if (mode == ORC_MODE_PHOTON && (!bs->off_idx || !bs->offsets)) return -1;
+    if (check_model(m)) return -1;
+    init_lf_d();
+    return f64 ? f64_run_pda(bs, n, args, P, m, mode, S, seed, b0, b1, hist, unit_out, nthreads)
+               : f32_run_pda(bs, n, args, P, m, mode, S, seed, b0, b1, hist, unit_out, nthreads);
+}
+
+int orc_run_refcompat(const orc_rc_bursts *bs, int32_t n, const float *args,
+                      const orc_model *m, int32_t S, uint64_t seed,
+                      int64_t b0, int64_t b1, uint64_t *hist, float *mcE,
+                      int32_t nthreads, int32_t f64) {
+    if (!bs || !args || !m) return -1;
+    if (n < 2 || n > ORC_MAXS) return -1;
+    if (S < 1 || b0 < 0 || b1 < b0 || b1 > bs->B) return -1;
+    if (check_model(m)) return -1;
+    init_lf_d();
+    return f64 ? f64_run_refcompat(bs, n, args, m, S, seed, b0, b1, hist, mcE, nthreads)
+               : f32_run_refcompat(bs, n, args, m, S, seed, b0, b1, hist, mcE, nthreads);
+}
+
+double orc_chi2(const uint64_t *hist, const float *ohist, int32_t nbins,
+                int32_t left_pad, int32_t S, int32_t n_states) {
+    int effN = nbins - left_pad;
+    double chi = 0.0;
+    for (int i = left_pad; i < nbins; ++i) {
+        if (hist[i] > 0) {
+            double mi = (double)hist[i] / (double)S;
+            double dlt = (double)ohist[i] - mi;
+            chi = chi + dlt * dlt / mi;
+        } else {
+            effN -= 1;
+        }
+    }
+    return chi / (double)(effN - n_states * (n_states + 1));
+}
+
+/* streamWorker.cpp:197-206, in its own float arithmetic */
+float orc_chi2_f32(const float *mhist, const float *ohist, int32_t nbins,
+                   int32_t left_pad, int32_t R, int32_t n_states) {
+    int effN = nbins - left_pad;
+    float chisqr = 0.0f;
+    for (int i = left_pad; i < nbins; ++i) {
+        if (mhist[i] > 0.0f) {
+            /* pow(float, int) is a double; the += rounds back to float */
+            float mr = mhist[i] / (float)R;
+            float d = ohist[i] - mr;
+            double term = pow((double)d, 2.0) / (double)mr;
+            chisqr = (float)((double)chisqr + term);
+        } else {
+            effN--;
+        }
+    }
+    return chisqr / (float)(effN - n_states * (n_states + 1));
+}
+
+void orc_bin_values(const float *x, int64_t n, int32_t nbins, float *hist_out) {
+    for (int i = 0; i < nbins; ++i) hist_out[i] = 0.0f;
+    for (int64_t k = 0; k < n; ++k) {
+        int b = ref_bin_d((double)x[k], nbins);
+        if (b >= 0) hist_out[b] += 1.0f;
+    }
+}
