@@ -1,0 +1,339 @@
+#!/usr/bin/env python
+"""Throughput of the photon-burst Monte-Carlo PDA hot path on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpda|reference]
+
+Metric: simulated bursts/s, 1 unit = one (parameter set, burst, MC sample)
+proximity-ratio draw. Workload (one step = one pass over it): photon_3state,
+100,000 seeded synthetic bursts, N = 30 + Geometric(mean 120) photons, T ~
+LogNormal(ln 1.5 ms, 0.5), sorted uniform arrival offsets (fp32), 3 states with
+log-uniform rates in [50,5000]/s, photon-by-photon state assignment, 100 MC
+samples per burst, fused 21-bin histogram + FP64 reduced chi-square.
+
+value: device-timed throughput with the burst store resident in HBM (CUDA
+events on the engine stream around each step; a 256 MB write flushes the L2
+between steps, outside the events). e2e: the same metric through the C ABI
+with pinned HOST buffers: each step uploads the burst store (+ device-side
+validation) and the parameters, runs, and reads back histogram + chi-square.
+
+--impl reference times the CPU restatement of the path (the reference has no
+CPU Monte-Carlo of its own) on the host cores of this machine, all threads.
+N > 1 (torchrun): independent replicas, one per GPU, max-over-ranks timing.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "sim bursts/s on 1 GB300"
+UNIT = "bursts/s"
+WORKLOAD = "photon_3state"
+B_FULL = 100_000
+SAMPLES = 100
+HELD_OUT_SEED = 0x0B5E
+# fixed cost model per unit of this workload (ALU ops): 25 per Philox word,
+# 16 per log, 40 per BTRD-class binomial, 2 per photon compare
+ALU_OPS_PER_UNIT = 1040.0
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="gpda", choices=["gpda", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--bursts", type=int, default=B_FULL)
+    return ap.parse_args()
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 100 ms."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_id):
+        self.gpu_id = gpu_id
+        self.samples = []
+        self.proc = None
+        self.marks = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100", "-i", str(self.gpu_id)],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append((time.monotonic(), [x.strip() for x in line.split(",")]))
+
+    def mark(self):
+        self.marks.append(time.monotonic())
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        t0, t1 = (self.marks + [0, 0])[:2] if len(self.marks) >= 2 else (0, 1e18)
+        inside = [s for t, s in self.samples if t0 <= t <= t1] or [s for _, s in self.samples[-3:]]
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        sm = [num(s[1]) for s in inside if num(s[1]) is not None]
+        smax = [num(s[2]) for s in inside if num(s[2]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in inside for i in range(4)
+                          if len(s) > 5 + i and s[5 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": reasons, "samples_in_timed_region": len(inside),
+                "power_w_max": max((num(s[3]) or 0.0) for s in inside)}
+
+
+def workload(B):
+    from gsmfretda_gb300 import synth
+    bs, n, args, md, S = synth.photon_3state(B=B, seed=2)
+    return bs, n, args, md, S
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured", float(d.get("sm_max_mhz", 2070.0))
+    except Exception:
+        return 6800.0, "fallback", 2070.0
+
+
+def cpu_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def oracle_rate(bs, n, args, md, S, b1, reps=1):
+    """Units/s of the CPU restatement (all host threads) on bursts [0, b1)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import build_oracle
+    build_oracle.build()
+    import orc
+    m = orc.model(**md)
+    th = cpu_threads()
+    best = 0.0
+    for r in range(reps):
+        t0 = time.perf_counter()
+        orc.run_pda(bs.N, bs.T, n, args, m, 1, S, 1000 + r, b0=0, b1=b1, off_idx=bs.off_idx,
+                    offsets=bs.offsets, nthreads=th)
+        dt = time.perf_counter() - t0
+        best = max(best, b1 * S / dt)
+    return best, th
+
+
+def run_reference(a):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    bs, n, args, md, S = workload(a.bursts)
+    sample_b = min(20_000, bs.B)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import build_oracle
+    build_oracle.build()
+    import orc
+    m = orc.model(**md)
+    th = cpu_threads()
+    for w in range(a.warmup):
+        orc.run_pda(bs.N, bs.T, n, args, m, 1, S, 500 + w, b0=0, b1=sample_b, off_idx=bs.off_idx,
+                    offsets=bs.offsets, nthreads=th)
+    t0 = time.perf_counter()
+    for k in range(a.steps):
+        orc.run_pda(bs.N, bs.T, n, args, m, 1, S, 900 + k, b0=0, b1=sample_b, off_idx=bs.off_idx,
+                    offsets=bs.offsets, nthreads=th)
+    dt = time.perf_counter() - t0
+    value = a.steps * sample_b * S / dt
+    sample = f"bursts [0,{sample_b}) of the workload x {S} samples per step"
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": a.gpus,
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 * dt / a.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded)",
+            "config": {"workload": WORKLOAD, "bursts": a.bursts, "samples": S, "states": n,
+                       "param_sets": 1, "mode": "photon-by-photon"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": th, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    a = parse()
+    if a.impl == "reference":
+        return run_reference(a)
+    import numpy as np
+    import torch
+
+    from gsmfretda_gb300 import build as gbuild
+    gbuild.build()
+    from gsmfretda_gb300.api import MODE_PHOTON, Engine
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    bs, n, args, md, S = workload(a.bursts)
+    units = bs.B * S
+    eng = Engine(local, **md)
+    eng.upload(bs)
+    # observed histogram: one draw per burst at a held-out seed
+    ohist, _ = eng.run_plain(MODE_PHOTON, n, args, 1, HELD_OUT_SEED)
+    eng.set_observed(ohist.astype(np.float32))
+
+    ext = torch.cuda.ExternalStream(eng.stream_handle, device=torch.device("cuda", local))
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+
+    def l2_flush():
+        with torch.cuda.stream(ext):
+            flush.zero_()
+
+    for w in range(a.warmup):
+        eng.launch(MODE_PHOTON, n, args, S, 10_000 + w)
+        l2_flush()
+    eng.synchronize()
+
+    gpu_index = local
+    try:
+        vis = os.environ.get("CUDA_VISIBLE_DEVICES")
+        if vis:
+            gpu_index = vis.split(",")[local]
+    except Exception:
+        pass
+    clocks = ClockSampler(gpu_index)
+    clocks.start()
+    time.sleep(0.3)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(a.steps)]
+    kern_ms = []
+    launches0 = eng.launch_count
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks.mark()
+    for k in range(a.steps):
+        ev[k][0].record(ext)
+        eng.launch(MODE_PHOTON, n, args, S, 20_000 + k)
+        ev[k][1].record(ext)
+        l2_flush()
+        kern_ms.append(eng.lib.gpda_kernel_ms(eng.ctx))
+    eng.synchronize()
+    torch.cuda.synchronize()
+    clocks.mark()
+    if dist:
+        dist.barrier()
+    launches = eng.launch_count - launches0
+    step_ms = [s.elapsed_time(e) for s, e in ev]
+    total_s = sum(step_ms) / 1e3
+    hist, chi2 = eng.fetch(1)
+    time.sleep(0.2)
+    clocks.stop()
+    if dist:
+        t = torch.tensor([total_s], device=f"cuda:{local}", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_s = float(t.item())
+    value = world * units * a.steps / total_s
+
+    # ---------------- end to end through the C ABI with pinned host buffers
+    pin = lambda x, dt: torch.from_numpy(np.ascontiguousarray(x, dtype=dt)).pin_memory().numpy()  # noqa: E731
+    hN, hT = pin(bs.N, np.int32), pin(bs.T, np.float32)
+    hOI, hOF = pin(bs.off_idx, np.int64), pin(bs.offsets, np.float32)
+    hA = pin(args, np.float32)
+    e2e_steps = max(3, min(a.steps, 50))
+    e2e_s = []
+    for k in range(e2e_steps + 2):
+        l2_flush()
+        eng.synchronize()
+        t0 = time.perf_counter()
+        eng.upload(N=hN, T=hT, off_idx=hOI, offsets=hOF)
+        h, c2 = eng.run_plain(MODE_PHOTON, n, hA, S, 30_000 + k)
+        t1 = time.perf_counter()
+        if k >= 2:
+            e2e_s.append(t1 - t0)
+    e2e_mean = sum(e2e_s) / len(e2e_s)
+    if dist:
+        t = torch.tensor([e2e_mean], device=f"cuda:{local}", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_mean = float(t.item())
+    h2d = hN.nbytes + hT.nbytes + hOI.nbytes + hOF.nbytes + hA.nbytes
+    d2h = 8 * md["nbins"] + 8 + 4
+
+    # ---------------- roofline of the dominant kernel (HBM side; the path is ALU bound)
+    kavg_ms = sum(kern_ms) / len(kern_ms)
+    alg_bytes = 4 * bs.B + 4 * bs.B + 8 * (bs.B + 1) + 4 * int(bs.off_idx[-1])
+    hbm_peak, peak_kind, sm_max = peaks()
+    achieved_gbs = alg_bytes / (kavg_ms * 1e-3) / 1e9
+    alu_peak = 152 * 128 * sm_max * 1e6 / 1e9          # FP32/INT32 lane-ops per s, in Gop/s
+    alu_achieved = units / (kavg_ms * 1e-3) * ALU_OPS_PER_UNIT / 1e9
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": 1e3 * total_s / a.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD, "bursts": bs.B, "samples": S, "states": n, "param_sets": 1,
+                   "mode": "photon-by-photon", "photons": int(bs.off_idx[-1]),
+                   "l2": "flushed between steps (256 MB write outside the timed events)",
+                   "parallelism": f"replicas x{world}"},
+        "e2e": {"value": world * units / e2e_mean, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": int(launches),
+        "clocks": clocks.summary(),
+        "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": achieved_gbs / hbm_peak, "traffic": None, "peak_kind": peak_kind,
+                     "algorithmic_bytes_per_launch": alg_bytes, "kernel_ms": kavg_ms,
+                     "alu": {"achieved": alu_achieved, "peak": alu_peak, "unit": "Gop/s",
+                             "frac": alu_achieved / alu_peak, "ops_per_unit": ALU_OPS_PER_UNIT}},
+        "chi2_last": float(chi2[0]),
+    }
+    if rank == 0 and world == 1 and not a.no_cpu_baseline:
+        rate, th = oracle_rate(bs, n, args, md, S, bs.B, reps=2)
+        line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": th, "kind": "port",
+                                "sample": f"full workload ({bs.B} bursts x {S} samples), best of 2"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    eng.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -36,7 +36,13 @@ struct gpda_ctx {
     float *dT = nullptr;
     int64_t *dOffIdx = nullptr;
     float *dOff = nullptr;
+    int64_t cap_B = 0;
+    int64_t cap_ph = 0;
     bool has_offsets = false;
+    unsigned int *dFlag = nullptr;
+    unsigned int *hFlag = nullptr;   // pinned
+    cudaEvent_t k0 = nullptr, k1 = nullptr;  // around the last MC kernel
+    bool timed = false;
     // observed histogram
     float *dObs = nullptr;
     bool has_obs = false;
@@ -191,7 +197,10 @@ int do_launch(gpda_ctx *c, int mode, int P, int n, const float *params, int64_t 
     a.bg_d = c->model.bg_d;
     size_t dyn = (mode == GPDA_MODE_PHOTON) ? sizeof(float) * kSmemCapFloats : 0;
     int grid = std::min<int64_t>(a.n_items, (int64_t)c->num_sms * c->blocks_per_sm[mode]);
+    CK(cudaEventRecord(c->k0, c->stream));
     CK(launch_pda(mode, a, grid, dyn, c->stream));
+    CK(cudaEventRecord(c->k1, c->stream));
+    c->timed = true;
     c->launches += 1;
     if (c->has_obs) {
         CK(launch_chi2(c->dHist, c->dObs, P, nbins, c->model.left_pad, S, n, c->dChi2, c->stream));
@@ -249,6 +258,10 @@ gpda_ctx *gpda_create(int32_t device, const gpda_model *m, int32_t *status) {
     if (bad(cudaMalloc(&c->dLimit, sizeof(unsigned long long)))) return nullptr;
     if (bad(cudaMemset(c->dLimit, 0, sizeof(unsigned long long)))) return nullptr;
     if (bad(cudaMalloc(&c->dObs, sizeof(float) * GPDA_MAX_BINS))) return nullptr;
+    if (bad(cudaMalloc(&c->dFlag, sizeof(unsigned int)))) return nullptr;
+    if (bad(cudaMallocHost(&c->hFlag, sizeof(unsigned int)))) return nullptr;
+    if (bad(cudaEventCreate(&c->k0))) return nullptr;
+    if (bad(cudaEventCreate(&c->k1))) return nullptr;
     if (bad(cudaEventRecord(c->params_ev, c->stream))) return nullptr;
     if (bad(pda_occupancy_blocks(0, 0, &c->blocks_per_sm[0]))) return nullptr;
     if (bad(pda_occupancy_blocks(1, sizeof(float) * kSmemCapFloats, &c->blocks_per_sm[1]))) return nullptr;
@@ -263,7 +276,10 @@ void gpda_destroy(gpda_ctx *c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     free_dev(c->dN); free_dev(c->dT); free_dev(c->dOffIdx); free_dev(c->dOff);
     free_dev(c->dObs); free_dev(c->dParams); free_dev(c->dHist); free_dev(c->dChi2);
-    free_dev(c->dWork); free_dev(c->dLimit); free_dev(c->dUnit);
+    free_dev(c->dWork); free_dev(c->dLimit); free_dev(c->dUnit); free_dev(c->dFlag);
+    if (c->hFlag) cudaFreeHost(c->hFlag);
+    if (c->k0) cudaEventDestroy(c->k0);
+    if (c->k1) cudaEventDestroy(c->k1);
     if (c->hParams) cudaFreeHost(c->hParams);
     if (c->hHist) cudaFreeHost(c->hHist);
     if (c->hChi2) cudaFreeHost(c->hChi2);
@@ -279,42 +295,56 @@ int32_t gpda_upload_bursts(gpda_ctx *c, const int32_t *N, const float *T, const 
     if (!c) return GPDA_ERR_ARG;
     if (B < 1 || B > (int64_t)INT32_MAX || !N || !T) return fail(c, GPDA_ERR_ARG, "B, N or T");
     if ((off_idx == nullptr) != (offsets == nullptr)) return fail(c, GPDA_ERR_ARG, "off_idx and offsets go together");
-    double sumN = 0.0;
-    for (int64_t b = 0; b < B; ++b) {
-        if (N[b] < 0 || N[b] > (1 << 21)) return fail(c, GPDA_ERR_ARG, "N out of [0, 2^21] at burst " + std::to_string(b));
-        if (!(T[b] >= 0.0f) || !std::isfinite(T[b])) return fail(c, GPDA_ERR_ARG, "T not finite and >= 0 at burst " + std::to_string(b));
-        sumN += N[b];
-    }
     int64_t nph = 0;
     if (off_idx) {
-        if (off_idx[0] != 0) return fail(c, GPDA_ERR_ARG, "off_idx[0] must be 0");
-        for (int64_t b = 0; b < B; ++b) {
-            if (off_idx[b + 1] - off_idx[b] != (int64_t)N[b]) return fail(c, GPDA_ERR_ARG, "off_idx inconsistent with N at burst " + std::to_string(b));
-            for (int64_t i = off_idx[b]; i < off_idx[b + 1]; ++i) {
-                if (!std::isfinite(offsets[i])) return fail(c, GPDA_ERR_ARG, "offset not finite");
-                if (i > off_idx[b] && offsets[i] < offsets[i - 1]) return fail(c, GPDA_ERR_ARG, "offsets not sorted in burst " + std::to_string(b));
-            }
-        }
+        if (off_idx[0] != 0 || off_idx[B] < 0) return fail(c, GPDA_ERR_ARG, "off_idx[0] must be 0 and off_idx[B] >= 0");
         nph = off_idx[B];
     }
     CK(cudaSetDevice(c->device));
     CK(cudaStreamSynchronize(c->stream));
-    free_dev(c->dN); free_dev(c->dT); free_dev(c->dOffIdx); free_dev(c->dOff);
-    c->dN = nullptr; c->dT = nullptr; c->dOffIdx = nullptr; c->dOff = nullptr;
     c->B = 0;
-    CK(cudaMalloc(&c->dN, sizeof(int32_t) * B));
-    CK(cudaMalloc(&c->dT, sizeof(float) * B));
+    // grow-only device store; contents are validated on the device below
+    if (B > c->cap_B) {
+        free_dev(c->dN); free_dev(c->dT); free_dev(c->dOffIdx);
+        c->dN = nullptr; c->dT = nullptr; c->dOffIdx = nullptr; c->cap_B = 0;
+        CK(cudaMalloc(&c->dN, sizeof(int32_t) * B));
+        CK(cudaMalloc(&c->dT, sizeof(float) * B));
+        CK(cudaMalloc(&c->dOffIdx, sizeof(int64_t) * (B + 1)));
+        c->cap_B = B;
+    }
+    if (off_idx && nph > c->cap_ph) {
+        free_dev(c->dOff);
+        c->dOff = nullptr; c->cap_ph = 0;
+        CK(cudaMalloc(&c->dOff, sizeof(float) * (nph + kOffPad)));
+        c->cap_ph = nph;
+    }
     CK(cudaMemcpyAsync(c->dN, N, sizeof(int32_t) * B, cudaMemcpyHostToDevice, c->stream));
     CK(cudaMemcpyAsync(c->dT, T, sizeof(float) * B, cudaMemcpyHostToDevice, c->stream));
     c->has_offsets = off_idx != nullptr;
     if (off_idx) {
-        CK(cudaMalloc(&c->dOffIdx, sizeof(int64_t) * (B + 1)));
-        CK(cudaMalloc(&c->dOff, sizeof(float) * (nph + kOffPad)));
         CK(cudaMemcpyAsync(c->dOffIdx, off_idx, sizeof(int64_t) * (B + 1), cudaMemcpyHostToDevice, c->stream));
         CK(cudaMemsetAsync(c->dOff + nph, 0, sizeof(float) * kOffPad, c->stream));
         if (nph > 0) CK(cudaMemcpyAsync(c->dOff, offsets, sizeof(float) * nph, cudaMemcpyHostToDevice, c->stream));
     }
+    CK(cudaMemsetAsync(c->dFlag, 0, sizeof(unsigned int), c->stream));
+    CK(launch_validate(c->dN, c->dT, off_idx ? c->dOffIdx : nullptr, off_idx ? c->dOff : nullptr, B,
+                       c->dFlag, c->num_sms, c->stream));
+    c->launches += 1;
+    CK(cudaMemcpyAsync(c->hFlag, c->dFlag, sizeof(unsigned int), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
+    unsigned f = *c->hFlag;
+    if (f) {
+        std::string why;
+        if (f & 1u) why += " N outside [0, 2^21];";
+        if (f & 2u) why += " T not finite and >= 0;";
+        if (f & 4u) why += " off_idx inconsistent with N;";
+        if (f & 8u) why += " offset not finite;";
+        if (f & 16u) why += " offsets not sorted within a burst;";
+        return fail(c, GPDA_ERR_ARG, "burst store rejected:" + why);
+    }
+    double sumN = 0.0;
+    if (off_idx) sumN = (double)nph;
+    else for (int64_t b = 0; b < B; ++b) sumN += N[b];
     c->B = B;
     c->nph = nph;
     c->mean_N = sumN / (double)B;
@@ -433,6 +463,15 @@ int32_t gpda_synchronize(gpda_ctx *c) {
 void *gpda_stream(gpda_ctx *c) { return c ? (void *)c->stream : nullptr; }
 
 int64_t gpda_launch_count(const gpda_ctx *c) { return c ? c->launches : 0; }
+
+float gpda_kernel_ms(gpda_ctx *c) {
+    if (!c || !c->timed) return -1.0f;
+    cudaSetDevice(c->device);
+    if (cudaEventSynchronize(c->k1) != cudaSuccess) return -1.0f;
+    float ms = -1.0f;
+    if (cudaEventElapsedTime(&ms, c->k0, c->k1) != cudaSuccess) return -1.0f;
+    return ms;
+}
 
 int64_t gpda_limit_hits(gpda_ctx *c) {
     if (!c) return GPDA_ERR_ARG;

@@ -76,6 +76,9 @@ cudaError_t launch_pda(int mode, const PdaArgs &a, int grid, size_t dyn_smem, cu
 cudaError_t launch_chi2(const unsigned long long *hist, const float *obs, int P, int nbins,
                         int left_pad, int S, int n_states, double *chi2, cudaStream_t st);
 cudaError_t launch_rc(const RcArgs &a, cudaStream_t st);
+cudaError_t launch_validate(const int32_t *N, const float *T, const int64_t *off_idx,
+                            const float *offsets, int64_t B, unsigned int *flag, int num_sms,
+                            cudaStream_t st);
 cudaError_t pda_occupancy_blocks(int mode, size_t dyn_smem, int *blocks_per_sm);
 cudaError_t pda_set_smem_limit(int mode, size_t dyn_smem);
 

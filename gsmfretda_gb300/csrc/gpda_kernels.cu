@@ -18,6 +18,8 @@
 //
 // No tensor cores: nothing here is a contraction. The work is INT32 (Philox)
 // and FP32 ALU bound; HBM traffic is the burst store read once per item.
+#include <algorithm>
+
 #include "gpda_device.cuh"
 #include "gpda_internal.h"
 
@@ -372,7 +374,50 @@ __global__ void __launch_bounds__(kThreads) rc_kernel(const RcArgs a) {
     if (lim) atomicAdd(a.limit_hits, (unsigned long long)lim);
 }
 
+// ---------------------------------------------------------------- burst-store validation
+
+// One warp per burst: photon counts in range, durations finite and >= 0,
+// off_idx consistent with N, offsets finite and sorted within the burst.
+// Sets bits of *flag (1: N, 2: T, 4: off_idx, 8: offset not finite, 16: unsorted).
+__global__ void validate_kernel(const int32_t *N, const float *T, const int64_t *off_idx,
+                                const float *offsets, int64_t B, unsigned int *flag) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    unsigned bad = 0u;
+    for (int64_t b = warp; b < B; b += nwarps) {
+        const int32_t nb = N[b];
+        const float tb = T[b];
+        if (lane == 0) {
+            if (nb < 0 || nb > (1 << 21)) bad |= 1u;
+            if (!(tb >= 0.0f) || !isfinite(tb)) bad |= 2u;
+        }
+        if (off_idx) {
+            const int64_t lo = off_idx[b], hi = off_idx[b + 1];
+            if (lane == 0 && hi - lo != (int64_t)nb) bad |= 4u;
+            if (hi - lo == (int64_t)nb && nb > 0) {
+                for (int64_t i = lo + lane; i < hi; i += 32) {
+                    const float x = offsets[i];
+                    if (!isfinite(x)) bad |= 8u;
+                    if (i > lo && x < offsets[i - 1]) bad |= 16u;
+                }
+            }
+        }
+    }
+    if (bad) atomicOr(flag, bad);
+}
+
 // ---------------------------------------------------------------- launchers
+
+cudaError_t launch_validate(const int32_t *N, const float *T, const int64_t *off_idx,
+                            const float *offsets, int64_t B, unsigned int *flag, int num_sms,
+                            cudaStream_t st) {
+    int64_t warps = B;
+    int64_t grid = std::min<int64_t>((warps * 32 + 255) / 256, (int64_t)num_sms * 8);
+    if (grid < 1) grid = 1;
+    validate_kernel<<<(unsigned)grid, 256, 0, st>>>(N, T, off_idx, offsets, B, flag);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_pda(int mode, const PdaArgs &a, int grid, size_t dyn_smem, cudaStream_t st) {
     if (mode == 0) pda_kernel<0><<<grid, kThreads, dyn_smem, st>>>(a);

@@ -87,7 +87,10 @@ const char *gpda_last_error(const gpda_ctx *ctx);
  * (src/mc.cu:456-521) for the pda model: N int32[B] photons per burst,
  * T float[B] durations (s), and for photon mode off_idx int64[B+1] prefix
  * offsets into offsets float[off_idx[B]] (sorted arrival offsets in [0,T],
- * seconds; checked). off_idx/offsets may be NULL for occupancy mode. */
+ * seconds). off_idx/offsets may be NULL for occupancy mode. The store is
+ * validated on the device (N in [0,2^21], T finite >= 0, off_idx consistent
+ * with N, offsets finite and sorted per burst); GPDA_ERR_ARG if not. Pinned
+ * host buffers make the copies asynchronous DMA. */
 int32_t gpda_upload_bursts(gpda_ctx *ctx, const int32_t *N, const float *T,
                            const int64_t *off_idx, const float *offsets, int64_t B);
 
@@ -142,6 +145,9 @@ int32_t gpda_synchronize(gpda_ctx *ctx);
 void *gpda_stream(gpda_ctx *ctx);
 /* Kernel launches issued so far on this context. */
 int64_t gpda_launch_count(const gpda_ctx *ctx);
+/* Device time (ms, CUDA events on the context stream) of the most recent
+ * Monte-Carlo kernel launch alone; waits for it. -1 if none. */
+float gpda_kernel_ms(gpda_ctx *ctx);
 /* Number of units whose segment/rejection loops hit their bound so far. */
 int64_t gpda_limit_hits(gpda_ctx *ctx);
 
