@@ -8,7 +8,8 @@ import ctypes as C
 import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libgpda.so")
+# GPDA_LIB points at another build of the same library (e.g. a variant being timed)
+LIB_PATH = os.environ.get("GPDA_LIB") or os.path.join(HERE, "libgpda.so")
 
 GPDA_OK = 0
 ERRORS = {-1: "GPDA_ERR_ARG", -2: "GPDA_ERR_SINGULAR", -3: "GPDA_ERR_CUDA",
@@ -74,6 +75,7 @@ SIGNATURES = {
     "gpda_mc_run_kernel": (_I32, [_VP, _I32, _I32]),
     "gpda_mc_streamQuery": (_I32, [_VP, _I32]),
     "gpda_mc_hmcE": (C.POINTER(C.c_float), [_VP, _I32]),
+    "gpda_mc_gpu_uuid": (_I32, [_VP, C.c_char_p]),
     "gpda_mc_set_hist_bins": (_I32, [_VP, _I32]),
     "gpda_mc_hist": (_I32, [_VP, _I32, _VP]),
 }

@@ -159,13 +159,18 @@ __device__ __forceinline__ float fc(float k) {
 }
 
 // ---------------------------------------------------------------- samplers
+// The sequential-search loops multiply by a table of reciprocals
+// inv[k] = 1.0f / k (k < 64, filled per CTA in shared memory) instead of
+// dividing: the search bounds keep k <= 51.
+constexpr int kInvTable = 64;
+
 // Binomial by sequential-search inversion (Kachitvichyanukul & Schmeiser
-// 1988); p <= 1/2, n p < 10.
-__device__ __noinline__ int binv(Rng &r, int n, float p, int &lim) {
+// 1988); p <= 1/2, n p < 10; logq = log(1-p) and rr = p/(1-p) as computed here.
+__device__ __forceinline__ int binv_pre(Rng &r, int n, float p, float logq, float rr, int &lim,
+                                        const float *inv) {
     float q = 1.0f - p;
     float nf = (float)n;
-    float qn = expf_(nf * logf_(q));
-    float rr = p / q;
+    float qn = expf_(nf * logq);
     float g = rr * (nf + 1.0f);
     float np = nf * p;
     float bf = np + 10.0f * sqrtf(np * q + 1.0f);
@@ -178,7 +183,7 @@ __device__ __noinline__ int binv(Rng &r, int n, float p, int &lim) {
             u = u - f;
             x += 1;
             if (x > bound) break;
-            f = f * (g / (float)x - rr);
+            f = f * (g * inv[x] - rr);
         }
         if (x <= bound) return x;
     }
@@ -186,9 +191,14 @@ __device__ __noinline__ int binv(Rng &r, int n, float p, int &lim) {
     return (int)np;
 }
 
+__device__ __forceinline__ int binv(Rng &r, int n, float p, int &lim, const float *inv) {
+    float q = 1.0f - p;
+    return binv_pre(r, n, p, logf_(q), p / q, lim, inv);
+}
+
 // Binomial by transformed rejection with decomposition (Hoermann 1993,
 // BTRD); p <= 1/2, n p >= 10.
-__device__ __noinline__ int btrd(Rng &r, int n, float p, int &lim) {
+__device__ __forceinline__ int btrd(Rng &r, int n, float p, int &lim) {
     float nf = (float)n;
     float q = 1.0f - p;
     float rr = p / q;
@@ -251,17 +261,28 @@ __device__ __noinline__ int btrd(Rng &r, int n, float p, int &lim) {
     return (int)m;
 }
 
-__device__ __forceinline__ int binom(Rng &r, int n, float p, int &lim) {
+__device__ __forceinline__ int binom(Rng &r, int n, float p, int &lim, const float *inv) {
     if (n <= 0 || !(p > 0.0f)) return 0;
     if (p >= 1.0f) return n;
     bool flip = p > 0.5f;
     float pp = flip ? 1.0f - p : p;
-    int x = ((float)n * pp < 10.0f) ? binv(r, n, pp, lim) : btrd(r, n, pp, lim);
+    int x = ((float)n * pp < 10.0f) ? binv(r, n, pp, lim, inv) : btrd(r, n, pp, lim);
+    return flip ? n - x : x;
+}
+
+// Same draw as binom(r, n, p) with the p-only constants precomputed on the
+// host per state (pp = min(p,1-p), logq = logf_(1-pp), rr = pp/(1-pp)).
+__device__ __forceinline__ int binom_pre(Rng &r, int n, float p, float pp, float logq, float rr,
+                                         int &lim, const float *inv) {
+    if (n <= 0 || !(p > 0.0f)) return 0;
+    if (p >= 1.0f) return n;
+    bool flip = p > 0.5f;
+    int x = ((float)n * pp < 10.0f) ? binv_pre(r, n, pp, logq, rr, lim, inv) : btrd(r, n, pp, lim);
     return flip ? n - x : x;
 }
 
 // Poisson by sequential-search inversion, lam < 10.
-__device__ __forceinline__ int pinv(Rng &r, float lam, int &lim) {
+__device__ __forceinline__ int pinv(Rng &r, float lam, int &lim, const float *inv) {
     float L = expf_(-lam);
     int bound = (int)(lam + 10.0f * sqrtf(lam) + 10.0f);
     for (int it = 0; it < kMaxRestart; ++it) {
@@ -272,7 +293,7 @@ __device__ __forceinline__ int pinv(Rng &r, float lam, int &lim) {
             u = u - f;
             k += 1;
             if (k > bound) break;
-            f = (f * lam) / (float)k;
+            f = (f * lam) * inv[k];
         }
         if (k <= bound) return k;
     }
@@ -286,7 +307,7 @@ __device__ __forceinline__ float logfact(float k) {
 }
 
 // Poisson by transformed rejection with squeeze (Hoermann 1993, PTRS), lam >= 10.
-__device__ __noinline__ int ptrs(Rng &r, float lam, int &lim) {
+__device__ __forceinline__ int ptrs(Rng &r, float lam, int &lim) {
     float slam = sqrtf(lam);
     float loglam = logf_(lam);
     float b = 0.931f + 2.53f * slam;
@@ -314,9 +335,9 @@ __device__ __noinline__ int ptrs(Rng &r, float lam, int &lim) {
     return (int)lam;
 }
 
-__device__ __forceinline__ int poisson(Rng &r, float lam, int &lim) {
+__device__ __forceinline__ int poisson(Rng &r, float lam, int &lim, const float *inv) {
     if (!(lam > 0.0f)) return 0;
-    return (lam < 10.0f) ? pinv(r, lam, lim) : ptrs(r, lam, lim);
+    return (lam < 10.0f) ? pinv(r, lam, lim, inv) : ptrs(r, lam, lim);
 }
 
 __device__ __forceinline__ float normal(Rng &r) {
@@ -331,7 +352,7 @@ __device__ __forceinline__ float root6(float x) {
 }
 
 // drawE (src/gen_rand.cuh:63-68): distance-broadened efficiency
-__device__ __noinline__ float broaden(Rng &r, float e, float r0, float v) {
+__device__ __forceinline__ float broaden(Rng &r, float e, float r0, float v) {
     float z = normal(r);
     float rd = z * v + r0 * root6(1.0f / e - 1.0f);
     float t = rd / r0;

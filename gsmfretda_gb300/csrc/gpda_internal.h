@@ -6,6 +6,10 @@
 namespace gpda {
 
 constexpr int kThreads = 256;       // threads per CTA of the MC kernels
+#ifndef GPDA_MIN_BLOCKS
+#define GPDA_MIN_BLOCKS 4
+#endif
+constexpr int kMinBlocks = GPDA_MIN_BLOCKS;  // resident CTAs per SM the register budget targets
 constexpr int kMaxTileBursts = 256; // bursts per work item
 constexpr int kHistBins = 1024;     // shared-memory histogram capacity
 
@@ -26,6 +30,12 @@ struct alignas(16) DevParams {
     float K[64];                  // rc: column-major n x n, leading dim n
     float Pi2j[64];               // rc: column-major jump probabilities
     float pinit[8];               // rc: unnormalised initial weights
+    // binomial constants per state, p = eps: pp = min(p, 1-p),
+    // logq = logf_(1-pp) (the device log, evaluated on the host), rr = pp/(1-pp)
+    float bpp[8];
+    float blogq[8];
+    float brr[8];
+    float pad2_[8];
 };
 static_assert(sizeof(DevParams) % 16 == 0, "DevParams must be 16-byte sized");
 constexpr int kParamWords = (int)(sizeof(DevParams) / 4);

@@ -50,92 +50,131 @@ __device__ __forceinline__ int lower_bound(const float *a, int lo, int hi, float
     return lo;
 }
 
-// Occupancy mode unit: Gillespie trajectory over [0,T] starting from the
-// stationary distribution, dwell = -ln(u)/k_exit, next state from the K
-// column; E_eff = sum_s f_s E_s; Poisson background (clipped), binomial split.
-__device__ __forceinline__ int unit_occ(const DevParams &P, float g, float ct, float r0,
-                                        float bga, float bgd, int Nb, float Tb, uint64_t seed,
-                                        uint32_t pw, uint32_t b, uint32_t s, int &lim) {
-    if (Nb <= 0) return -1;
+// One (burst, sample) unit in flight on a lane. The trajectory advances one
+// dwell segment per step so that a lane whose unit is finished can take the
+// next unit at once instead of idling until the slowest lane of its warp is
+// done (trajectory lengths vary from 1 to tens of segments).
+struct Unit {
     Rng r;
-    r.init(seed, pw, b, s);
-    const int n = P.n;
-    int st = cat_draw(P.init_cdf, n, r.u01());
-    float eeff;
-    if (Tb > 0.0f) {
-        float t = 0.0f, acc = 0.0f;
-        for (int seg = 0;; ++seg) {
-            float u = r.u01();
-            float tau = (P.kexit[st] > 0.0f) ? (-logf_(u)) * P.inv_kexit[st] : kInf;
-            float tn = t + tau;
-            bool cut = seg == kMaxSeg - 1;
-            bool last = !(tn < Tb) || cut;
-            if (cut && tn < Tb) lim += 1;
-            float dt = last ? Tb - t : tn - t;
-            float es = P.E[st];
-            if (P.V[st] > 0.0f) es = broaden(r, es, r0, P.V[st]);
-            acc = fmaf(dt, es, acc);
-            if (last) break;
-            t = tn;
-            st = jump_draw(P.jump_cdf + st * 8, n, st, r.u01());
-        }
-        eeff = acc / Tb;
-    } else {
-        eeff = P.E[st];
-    }
-    int Ba = poisson(r, bga * Tb, lim);
-    if (Ba > Nb) Ba = (int)floorf((float)Nb * r.u01());
-    int rem = Nb - Ba;
-    int Bd = poisson(r, bgd * Tb, lim);
-    if (Bd > rem) Bd = (int)floorf((float)rem * r.u01());
-    int ns = rem - Bd;
-    return binom(r, ns, eps_of(eeff, g, ct), lim) + Ba;
+    float t, acc, Tb;
+    int st, lo, A, seg, Nb;
+    int lb, s;          // tile-local burst, sample
+    int obase;          // staged: offset of the burst in shared memory
+    bool done;
+};
+
+__device__ __forceinline__ void unit_begin(Unit &U, const DevParams &P, int u, int S, int64_t tb0,
+                                           const int32_t *sN, const float *sT, uint64_t seed,
+                                           uint32_t pw) {
+    U.lb = u / S;
+    U.s = u - U.lb * S;
+    U.Nb = sN[U.lb];
+    U.Tb = sT[U.lb];
+    U.r.init(seed, pw, (uint32_t)(tb0 + U.lb), (uint32_t)U.s);
+    U.t = 0.0f;
+    U.acc = 0.0f;
+    U.lo = 0;
+    U.A = 0;
+    U.seg = 0;
+    U.done = U.Nb <= 0;
+    if (U.done) { U.A = -1; return; }
+    U.st = cat_draw(P.init_cdf, P.n, U.r.u01());
 }
 
-// Photon mode unit: each photon takes the state at its arrival offset; per
-// dwell segment with photons, Poisson background then Binomial(signal, eps).
-__device__ __forceinline__ int unit_pho(const DevParams &P, float g, float ct, float r0,
-                                        float bga, float bgd, int Nb, float Tb,
-                                        const float *offs, uint64_t seed, uint32_t pw,
-                                        uint32_t b, uint32_t s, int &lim) {
-    if (Nb <= 0) return -1;
-    Rng r;
-    r.init(seed, pw, b, s);
-    const int n = P.n;
-    int st = cat_draw(P.init_cdf, n, r.u01());
-    float t = 0.0f;
-    int lo = 0, A = 0;
-    for (int seg = 0;; ++seg) {
-        float u = r.u01();
+// Background of one window (Poisson, clipped as draw_P_B_Tr does,
+// src/gen_rand.cuh:92-107), acceptor channel first; returns the acceptor
+// background, writes the remaining signal photons to *sig.
+__device__ __forceinline__ int background(Rng &r, int navail, float lam_a, float lam_d, int *sig,
+                                          int &lim, const float *inv) {
+    int B[2];
+    int avail = navail;
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+        int x = poisson(r, c == 0 ? lam_a : lam_d, lim, inv);
+        if (x > avail) x = (int)floorf((float)avail * r.u01());
+        B[c] = x;
+        avail -= x;
+    }
+    *sig = avail;
+    return B[0];
+}
+
+// Photon mode: one dwell segment. Photons whose arrival offset falls in the
+// segment take its state; Poisson background then Binomial(signal, eps_state).
+__device__ __forceinline__ bool step_pho(Unit &U, const DevParams &P, const float *offs, float g,
+                                         float ct, float r0, float bga, float bgd, int &lim,
+                                         const float *inv) {
+    float u = U.r.u01();
+    const int st = U.st;
+    float tau = (P.kexit[st] > 0.0f) ? (-logf_(u)) * P.inv_kexit[st] : kInf;
+    float tn = U.t + tau;
+    bool cut = U.seg == kMaxSeg - 1;
+    bool last = !(tn < U.Tb) || cut;
+    if (cut && tn < U.Tb) lim += 1;
+    int hi;
+    float dt;
+    if (last) { hi = U.Nb; dt = U.Tb - U.t; }
+    else { hi = lower_bound(offs, U.lo, U.Nb, tn); dt = tn - U.t; }
+    int nk = hi - U.lo;
+    if (nk > 0) {
+        int sig;
+        if (P.V[st] > 0.0f) {
+            float ek = eps_of(broaden(U.r, P.E[st], r0, P.V[st]), g, ct);
+            int ba = background(U.r, nk, bga * dt, bgd * dt, &sig, lim, inv);
+            U.A += binom(U.r, sig, ek, lim, inv) + ba;
+        } else {
+            int ba = background(U.r, nk, bga * dt, bgd * dt, &sig, lim, inv);
+            U.A += binom_pre(U.r, sig, P.eps[st], P.bpp[st], P.blogq[st], P.brr[st], lim, inv) + ba;
+        }
+    }
+    U.lo = hi;
+    if (last) return true;
+    U.t = tn;
+    U.st = jump_draw(P.jump_cdf + st * 8, P.n, st, U.r.u01());
+    U.seg += 1;
+    return false;
+}
+
+// Occupancy mode: one dwell segment; the last one also draws the background
+// and the single binomial split with the occupancy-weighted efficiency.
+__device__ __forceinline__ bool step_occ(Unit &U, const DevParams &P, float g, float ct, float r0,
+                                         float bga, float bgd, int &lim, const float *inv) {
+    bool last = true;
+    if (U.Tb > 0.0f) {
+        float u = U.r.u01();
+        const int st = U.st;
         float tau = (P.kexit[st] > 0.0f) ? (-logf_(u)) * P.inv_kexit[st] : kInf;
-        float tn = t + tau;
-        bool cut = seg == kMaxSeg - 1;
-        bool last = !(tn < Tb) || cut;
-        if (cut && tn < Tb) lim += 1;
-        int hi;
-        float dt;
-        if (last) { hi = Nb; dt = Tb - t; }
-        else { hi = lower_bound(offs, lo, Nb, tn); dt = tn - t; }
-        int nk = hi - lo;
-        if (nk > 0) {
-            float ek = P.eps[st];
-            if (P.V[st] > 0.0f) ek = eps_of(broaden(r, P.E[st], r0, P.V[st]), g, ct);
-            int Ba = poisson(r, bga * dt, lim);
-            if (Ba > nk) Ba = (int)floorf((float)nk * r.u01());
-            int rem = nk - Ba;
-            int Bd = poisson(r, bgd * dt, lim);
-            if (Bd > rem) Bd = (int)floorf((float)rem * r.u01());
-            A += binom(r, rem - Bd, ek, lim) + Ba;
+        float tn = U.t + tau;
+        bool cut = U.seg == kMaxSeg - 1;
+        last = !(tn < U.Tb) || cut;
+        if (cut && tn < U.Tb) lim += 1;
+        float dt = last ? U.Tb - U.t : tn - U.t;
+        float es = P.E[st];
+        if (P.V[st] > 0.0f) es = broaden(U.r, es, r0, P.V[st]);
+        U.acc = fmaf(dt, es, U.acc);
+        if (!last) {
+            U.t = tn;
+            U.st = jump_draw(P.jump_cdf + st * 8, P.n, st, U.r.u01());
+            U.seg += 1;
+            return false;
         }
-        lo = hi;
-        if (last) break;
-        t = tn;
-        st = jump_draw(P.jump_cdf + st * 8, n, st, r.u01());
     }
-    return A;
+    float eeff = (U.Tb > 0.0f) ? U.acc / U.Tb : P.E[U.st];
+    int sig;
+    int ba = background(U.r, U.Nb, bga * U.Tb, bgd * U.Tb, &sig, lim, inv);
+    U.A = binom(U.r, sig, eps_of(eeff, g, ct), lim, inv) + ba;
+    return true;
 }
 
-// warp-aggregated shared-memory histogram increment (bin < 0: no count)
+// warp-aggregated shared-memory histogram increment; all 32 lanes call it
+// (bin < 0: no count)
+__device__ __forceinline__ void hist_add_warp(unsigned int *sh, int bin) {
+    unsigned peers = __match_any_sync(0xffffffffu, bin);
+    int leader = __ffs(peers) - 1;
+    if ((int)(threadIdx.x & 31) == leader && bin >= 0) atomicAdd(&sh[bin], (unsigned)__popc(peers));
+}
+
+// warp-aggregated shared-memory histogram increment from divergent code
 __device__ __forceinline__ void hist_add(unsigned int *sh, int bin) {
     unsigned mask = __activemask();
     unsigned peers = __match_any_sync(mask, bin);
@@ -144,7 +183,7 @@ __device__ __forceinline__ void hist_add(unsigned int *sh, int bin) {
 }
 
 template <int MODE>
-__global__ void __launch_bounds__(kThreads) pda_kernel(const PdaArgs a) {
+__global__ void __launch_bounds__(kThreads, kMinBlocks) pda_kernel(const PdaArgs a) {
     extern __shared__ float4 s_ph4[];
     float *s_ph = reinterpret_cast<float *>(s_ph4);
     __shared__ DevParams sp;
@@ -154,10 +193,18 @@ __global__ void __launch_bounds__(kThreads) pda_kernel(const PdaArgs a) {
     __shared__ unsigned int sh[kHistBins];
     __shared__ int s_item;
     __shared__ int s_staged;
+    __shared__ int s_next;
+    __shared__ float s_inv[kInvTable];
     const int tid = threadIdx.x;
+    const int lane = tid & 31;
+    if (tid < kInvTable) s_inv[tid] = tid > 0 ? 1.0f / (float)tid : 0.0f;
+    const unsigned lt_mask = (1u << lane) - 1u;
     int lim = 0;
     for (;;) {
-        if (tid == 0) s_item = (int)atomicAdd(a.work, 1u);
+        if (tid == 0) {
+            s_item = (int)atomicAdd(a.work, 1u);
+            s_next = kThreads;
+        }
         __syncthreads();
         const int item = s_item;
         if (item >= a.n_items) break;
@@ -194,28 +241,46 @@ __global__ void __launch_bounds__(kThreads) pda_kernel(const PdaArgs a) {
         __syncthreads();
         const int units = nb * a.S;
         const bool staged = (MODE == 1) && s_staged;
-        for (int u = tid; u < units; u += kThreads) {
-            const int lb = u / a.S;
-            const int s = u - lb * a.S;
-            const int64_t b = tb0 + lb;
-            const int Nb = sN[lb];
-            const float Tb = sT[lb];
-            int A;
-            if (MODE == 0) {
-                A = unit_occ(sp, a.gamma, a.ct, a.r0, a.bg_a, a.bg_d, Nb, Tb, a.seed,
-                             a.pbase + (uint32_t)p, (uint32_t)b, (uint32_t)s, lim);
-            } else {
-                const float *offs = staged ? (s_ph + sOff[lb]) : (a.offsets + a.off_idx[b]);
-                A = unit_pho(sp, a.gamma, a.ct, a.r0, a.bg_a, a.bg_d, Nb, Tb, offs, a.seed,
-                             a.pbase + (uint32_t)p, (uint32_t)b, (uint32_t)s, lim);
-            }
-            if (a.unit_out) a.unit_out[((int64_t)p * (a.b1 - a.b0) + (b - a.b0)) * a.S + s] = A;
+        const uint32_t pw = a.pbase + (uint32_t)p;
+        Unit U;
+        bool active = tid < units;
+        if (active) unit_begin(U, sp, tid, a.S, tb0, sN, sT, a.seed, pw);
+        while (__any_sync(0xffffffffu, active)) {
+            bool fin = false;
             int bin = -1;
-            if (Nb > 0 && A >= 0) {
-                unsigned v = (unsigned)A * (unsigned)a.nbins / (unsigned)Nb;
-                bin = v >= (unsigned)a.nbins ? a.nbins - 1 : (int)v;
+            if (active) {
+                fin = U.done;
+                if (!fin) {
+                    if (MODE == 0) {
+                        fin = step_occ(U, sp, a.gamma, a.ct, a.r0, a.bg_a, a.bg_d, lim, s_inv);
+                    } else {
+                        const float *offs = staged ? (s_ph + sOff[U.lb]) : (a.offsets + a.off_idx[tb0 + U.lb]);
+                        fin = step_pho(U, sp, offs, a.gamma, a.ct, a.r0, a.bg_a, a.bg_d, lim, s_inv);
+                    }
+                }
+                if (fin) {
+                    const int64_t b = tb0 + U.lb;
+                    if (a.unit_out) a.unit_out[((int64_t)p * (a.b1 - a.b0) + (b - a.b0)) * a.S + U.s] = U.A;
+                    if (U.Nb > 0 && U.A >= 0) {
+                        unsigned v = (unsigned)U.A * (unsigned)a.nbins / (unsigned)U.Nb;
+                        bin = v >= (unsigned)a.nbins ? a.nbins - 1 : (int)v;
+                    }
+                }
             }
-            hist_add(sh, bin);
+            hist_add_warp(sh, bin);
+            // lanes whose unit finished take the next units of the tile
+            const unsigned need = __ballot_sync(0xffffffffu, fin);
+            if (need) {
+                const int leader = __ffs(need) - 1;
+                int base = 0;
+                if (lane == leader) base = atomicAdd(&s_next, __popc(need));
+                base = __shfl_sync(0xffffffffu, base, leader);
+                if (fin) {
+                    const int u = base + __popc(need & lt_mask);
+                    active = u < units;
+                    if (active) unit_begin(U, sp, u, a.S, tb0, sN, sT, a.seed, pw);
+                }
+            }
         }
         __syncthreads();
         for (int i = tid; i < a.nbins; i += kThreads) {
@@ -278,8 +343,9 @@ __device__ __forceinline__ int64_t f2i64(double v) {
 }
 
 // draw_P_B_Tr (gen_rand.cuh:92-107) for one time bin
-__device__ __forceinline__ float bg_clip(Rng &r, float tot, float tdiff, float rate, int &lim) {
-    int sv = poisson(r, tdiff * rate, lim);
+__device__ __forceinline__ float bg_clip(Rng &r, float tot, float tdiff, float rate, int &lim,
+                                         const float *inv) {
+    int sv = poisson(r, tdiff * rate, lim, inv);
     if ((float)sv <= tot) return (float)sv;
     return floorf(tot * r.u01());
 }
@@ -287,7 +353,9 @@ __device__ __forceinline__ float bg_clip(Rng &r, float tot, float tdiff, float r
 __global__ void __launch_bounds__(kThreads) rc_kernel(const RcArgs a) {
     __shared__ DevParams sp;
     __shared__ unsigned int sh[kHistBins];
+    __shared__ float s_inv[kInvTable];
     const int tid = threadIdx.x;
+    if (tid < kInvTable) s_inv[tid] = tid > 0 ? 1.0f / (float)tid : 0.0f;
     {
         const uint32_t *src = reinterpret_cast<const uint32_t *>(a.params);
         uint32_t *dst = reinterpret_cast<uint32_t *>(&sp);
@@ -338,13 +406,13 @@ __global__ void __launch_bounds__(kThreads) rc_kernel(const RcArgs a) {
                     } else {
                         float tdiff = (float)(bin1 - bin0) * clk;
                         float rf_ia = (1.0f - dea) * (float)f_ia;
-                        float bga = bg_clip(r, rf_ia, tdiff, a.bg_ad_rate, lim);
+                        float bga = bg_clip(r, rf_ia, tdiff, a.bg_ad_rate, lim, s_inv);
                         float rf_id = (gam - cht) * (float)f_id;
-                        float bgd = bg_clip(r, rf_id, tdiff, a.bg_dd_rate, lim);
+                        float bgd = bg_clip(r, rf_id, tdiff, a.bg_dd_rate, lim, s_inv);
                         f_i = floorf((float)((double)(f_if - bgd - bga) + 0.5));
                     }
                     float de = broaden(r, sp.E[si], r0, sp.V[si]);
-                    ai = binom(r, (int)f_i, de, lim);
+                    ai = binom(r, (int)f_i, de, lim, s_inv);
                     break;
                 }
                 if (ddx > 0) sdd = 1;

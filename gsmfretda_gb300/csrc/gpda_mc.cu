@@ -165,6 +165,14 @@ int32_t gpda_mc_set_model(gpda_mc *m, const gpda_model *mm) {
     return GPDA_OK;
 }
 
+int32_t gpda_mc_gpu_uuid(gpda_mc *m, char *out) {
+    if (!m || !out) return GPDA_ERR_ARG;
+    cudaDeviceProp prop;
+    MCK(cudaGetDeviceProperties(&prop, m->devid));
+    std::memcpy(out, prop.uuid.bytes, 16);
+    return GPDA_OK;
+}
+
 int32_t gpda_mc_set_hist_bins(gpda_mc *m, int32_t nbins) {
     if (!m || nbins < 1 || nbins > GPDA_MAX_BINS) return mfail(m, GPDA_ERR_ARG, "nbins");
     m->nbins = nbins;

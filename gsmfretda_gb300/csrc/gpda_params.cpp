@@ -12,6 +12,7 @@
 //                 genMatP (:39-53) in the reference's float operation order.
 // All FP64 work is rounded once to FP32. Compiled with -ffp-contract=off.
 #include <cmath>
+#include <cstdint>
 #include <cstring>
 
 #include "gpda_internal.h"
@@ -19,6 +20,35 @@
 namespace gpda {
 
 namespace {
+
+// The device's logf_ (gpda_device.cuh), evaluated on the host with the same
+// operation order so that precomputed constants are the device's bits.
+float dev_logf(float x) {
+    if (x != x) return x;
+    if (x < 0.0f) return NAN;
+    if (x == 0.0f) return -INFINITY;
+    if (x == INFINITY) return x;
+    uint32_t bits;
+    std::memcpy(&bits, &x, 4);
+    int e = 0;
+    if ((bits >> 23) == 0u) {
+        x = x * 0x1p24f;
+        std::memcpy(&bits, &x, 4);
+        e = -24;
+    }
+    e += (int)(bits >> 23) - 127;
+    uint32_t mb = (bits & 0x007FFFFFu) | 0x3F800000u;
+    float m;
+    std::memcpy(&m, &mb, 4);
+    if (m > 0x1.6a09e6p+0f) { m = m * 0.5f; e += 1; }
+    float f = m - 1.0f;
+    float s = f / (2.0f + f);
+    float z = s * s;
+    float poly = std::fmaf(z, std::fmaf(z, std::fmaf(z, 0x1.c71c72p-3f, 0x1.24924ap-2f), 0x1.99999ap-2f), 0x1.555556p-1f);
+    float lm = std::fmaf(s * z, poly, 2.0f * s);
+    float ef = (float)e;
+    return std::fmaf(ef, 0x1.62e430p-1f, std::fmaf(ef, -0x1.05c610p-29f, lm));
+}
 
 inline float koff(const float *k, int n, int i, int j) {
     return (i < j) ? k[i * (n - 1) + j - 1] : k[i * (n - 1) + j];
@@ -110,6 +140,12 @@ int build_params(int n, const float *args, float gamma, float ct, bool need_pi, 
         float om = 1.0f - e;
         float num = gamma * e + ct * om;
         out->eps[i] = num / (num + om);
+        float p = out->eps[i];
+        float pp = (p > 0.5f) ? 1.0f - p : p;
+        float q = 1.0f - pp;
+        out->bpp[i] = pp;
+        out->blogq[i] = dev_logf(q);
+        out->brr[i] = pp / q;
         for (int j = 0; j < n; ++j) out->jump_cdf[i * 8 + j] = (float)jcdf[i * 8 + j];
     }
     // reference float tables (leading dimension n)

@@ -199,6 +199,9 @@ int32_t gpda_mc_run_kernel(gpda_mc *mc, int32_t N, int32_t sid);
 int32_t gpda_mc_streamQuery(gpda_mc *mc, int32_t sid);
 /* mc::hmcE[sid] (mc.hpp:83): pinned host results of the last run_kernel. */
 float *gpda_mc_hmcE(gpda_mc *mc, int32_t sid);
+/* The 16 raw bytes of the device UUID into out[16] (mc::gpuuuid, filled by
+ * showGPUsInfo, src/mc.cu:43-49; genuid formats them as hex). */
+int32_t gpda_mc_gpu_uuid(gpda_mc *mc, char *out);
 /* Histogram bins used by the fused on-device histogram (fretHistNum, -f). */
 int32_t gpda_mc_set_hist_bins(gpda_mc *mc, int32_t nbins);
 /* Device-binned histogram of the last completed run on stream sid (nbins

@@ -316,6 +316,10 @@ static inline int ref_bin_d(double z, int nbins) {
     return -1;
 }
 
+/* reciprocal tables of the sequential-search loops: 1.0f/k and 1.0/k */
+static float inv_tab_f[64];
+static double inv_tab_d[64];
+
 #define ORC_MAX_SEG 65536
 #define ORC_MAX_RESTART 256
 
@@ -334,6 +338,7 @@ static inline int ref_bin_d(double z, int nbins) {
 #define INFR INFINITY
 #define FC_T FC_TAB
 #define LF_T LF_TAB
+#define INV_T inv_tab_f
 #define PFX(x) f32_##x
 #include "gpda_oracle_core.inc"
 #undef REAL
@@ -349,6 +354,7 @@ static inline int ref_bin_d(double z, int nbins) {
 #undef INFR
 #undef FC_T
 #undef LF_T
+#undef INV_T
 #undef PFX
 
 /* FP64 transcription on the same counters. */
@@ -367,6 +373,7 @@ static double cos2pi_d(double u) { return cos(6.283185307179586 * u); }
 #define INFR ((double)INFINITY)
 #define FC_T FC_TAB_D
 #define LF_T lf_tab_d
+#define INV_T inv_tab_d
 #define PFX(x) f64_##x
 #include "gpda_oracle_core.inc"
 
@@ -374,6 +381,10 @@ static void init_lf_d(void) {
     static int done = 0;
     if (done) return;
     for (int k = 0; k < 10; ++k) lf_tab_d[k] = lgamma((double)k + 1.0);
+    for (int k = 0; k < 64; ++k) {
+        inv_tab_f[k] = k > 0 ? 1.0f / (float)k : 0.0f;
+        inv_tab_d[k] = k > 0 ? 1.0 / (double)k : 0.0;
+    }
     done = 1;
 }
 

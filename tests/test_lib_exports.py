@@ -39,7 +39,7 @@ def test_library_is_in_tree_and_loaded_from_there(gpda_lib):
 
 def test_host_only_entry_points(gpda_lib):
     assert gpda_lib.gpda_version().startswith(b"gpda")
-    assert gpda_lib.gpda_params_size() == 252
+    assert gpda_lib.gpda_params_size() == 284
     from gsmfretda_gb300._lib import GpdaModel
     m = GpdaModel()
     gpda_lib.gpda_model_defaults(C.byref(m))
@@ -48,8 +48,6 @@ def test_host_only_entry_points(gpda_lib):
 
 
 def test_missing_library_fails_loudly(tmp_path, monkeypatch):
-    import importlib
-
     import gsmfretda_gb300._lib as L
     monkeypatch.setattr(L, "LIB_PATH", str(tmp_path / "absent.so"))
     monkeypatch.setattr(L, "_lib", None)
@@ -58,4 +56,3 @@ def test_missing_library_fails_loudly(tmp_path, monkeypatch):
         raise AssertionError("load() must raise without the CUDA library")
     except ImportError as e:
         assert "no CPU fallback" in str(e)
-    importlib.reload(L)

@@ -57,8 +57,9 @@ def test_product_and_oracle_tables_identical(gpda_lib, orc, n):
     m = orc.model()
     f, _, _ = product_tables(n, args)
     o = np.frombuffer(bytes(orc.build_params(n, args, m)), dtype=np.float32)
-    mask = np.ones(f.size, dtype=bool)
-    mask[OFF["anyV"]] = False                                   # product-only flag word
+    f = f[:o.size]                      # the product appends precomputed binomial constants
+    mask = np.ones(o.size, dtype=bool)
+    mask[OFF["anyV"]] = False           # product-only flag word
     np.testing.assert_array_equal(f.view(np.uint32)[mask], o.view(np.uint32)[mask])
 
 
@@ -70,6 +71,23 @@ def test_stationary_distribution(gpda_lib, n):
     pi = np.diff(np.concatenate([[0.0], cdf]))
     assert abs(cdf[-1] - 1.0) < 1e-6
     assert np.abs(K.astype(np.float64) @ pi).max() < 1e-4 * np.abs(K).max()
+
+
+def test_precomputed_binomial_constants(gpda_lib, orc):
+    n = 5
+    args = rand_args(n, 9)
+    f, _, _ = product_tables(n, args)
+    eps = f[OFF["eps"]:OFF["eps"] + n]
+    pp = f[252:252 + n]
+    logq = f[260:260 + n]
+    rr = f[268:268 + n]
+    L = orc.lib()
+    for i in range(n):
+        want_pp = np.float32(1.0) - eps[i] if eps[i] > 0.5 else eps[i]
+        q = np.float32(1.0) - want_pp
+        assert pp[i] == want_pp
+        assert logq[i] == np.float32(L.orc_logf(float(q)))   # same FP32 log on both sides
+        assert rr[i] == np.float32(want_pp / q)
 
 
 def test_exit_rates_and_jump_cdf(gpda_lib):
