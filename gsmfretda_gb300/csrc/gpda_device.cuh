@@ -58,6 +58,10 @@ struct Rng {
         ++idx;
         return r;
     }
+    // The next draw starts a fresh block (the rest of the current one is
+    // discarded): keeps block generation at the same program point for all
+    // lanes of a warp.
+    __device__ __forceinline__ void align() { idx = 4; }
     // uniform on (0,1]: ((x >> 8) + 1) * 2^-24, exact
     __device__ __forceinline__ float u01() {
         return (float)((next() >> 8) + 1u) * 5.9604644775390625e-08f;
@@ -173,19 +177,28 @@ __device__ __forceinline__ int binv_pre(Rng &r, int n, float p, float logq, floa
     float qn = expf_(nf * logq);
     float g = rr * (nf + 1.0f);
     float np = nf * p;
-    float bf = np + 10.0f * sqrtf(np * q + 1.0f);
-    int bound = (bf < nf) ? (int)bf : n;
+    // bound = min(n, np + 10 sqrt(np q + 1)) >= min(n, 10): evaluated only
+    // once the search passes min(n, 10)
+    const int x10 = n < 10 ? n : 10;
+    int bound = -1;
     for (int it = 0; it < kMaxRestart; ++it) {
         int x = 0;
         float f = qn;
         float u = r.u01();
+        bool over = false;
         while (u > f) {
             u = u - f;
             x += 1;
-            if (x > bound) break;
+            if (x > x10) {
+                if (bound < 0) {
+                    float bf = np + 10.0f * sqrtf(np * q + 1.0f);
+                    bound = (bf < nf) ? (int)bf : n;
+                }
+                if (x > bound) { over = true; break; }
+            }
             f = f * (g * inv[x] - rr);
         }
-        if (x <= bound) return x;
+        if (!over) return x;
     }
     lim += 1;
     return (int)np;
@@ -284,18 +297,23 @@ __device__ __forceinline__ int binom_pre(Rng &r, int n, float p, float pp, float
 // Poisson by sequential-search inversion, lam < 10.
 __device__ __forceinline__ int pinv(Rng &r, float lam, int &lim, const float *inv) {
     float L = expf_(-lam);
-    int bound = (int)(lam + 10.0f * sqrtf(lam) + 10.0f);
+    // bound = lam + 10 sqrt(lam) + 10 >= 10: evaluated only once k passes 10
+    int bound = -1;
     for (int it = 0; it < kMaxRestart; ++it) {
         int k = 0;
         float f = L;
         float u = r.u01();
+        bool over = false;
         while (u > f) {
             u = u - f;
             k += 1;
-            if (k > bound) break;
+            if (k > 10) {
+                if (bound < 0) bound = (int)(lam + 10.0f * sqrtf(lam) + 10.0f);
+                if (k > bound) { over = true; break; }
+            }
             f = (f * lam) * inv[k];
         }
-        if (k <= bound) return k;
+        if (!over) return k;
     }
     lim += 1;
     return (int)lam;

@@ -63,9 +63,8 @@ struct Unit {
     bool done;
 };
 
-__device__ __forceinline__ void unit_begin(Unit &U, const DevParams &P, int u, int S, int64_t tb0,
-                                           const int32_t *sN, const float *sT, uint64_t seed,
-                                           uint32_t pw) {
+__device__ __forceinline__ void unit_begin(Unit &U, int u, int S, int64_t tb0, const int32_t *sN,
+                                           const float *sT, uint64_t seed, uint32_t pw) {
     U.lb = u / S;
     U.s = u - U.lb * S;
     U.Nb = sN[U.lb];
@@ -76,9 +75,16 @@ __device__ __forceinline__ void unit_begin(Unit &U, const DevParams &P, int u, i
     U.lo = 0;
     U.A = 0;
     U.seg = 0;
+    U.st = 0;
     U.done = U.Nb <= 0;
-    if (U.done) { U.A = -1; return; }
-    U.st = cat_draw(P.init_cdf, P.n, U.r.u01());
+    if (U.done) U.A = -1;
+}
+
+// State of segment U.seg: the stationary draw for the first segment, the jump
+// from the previous state afterwards (one word, the first of the step).
+__device__ __forceinline__ int next_state(const Unit &U, const DevParams &P, float us) {
+    return (U.seg == 0) ? cat_draw(P.init_cdf, P.n, us)
+                        : jump_draw(P.jump_cdf + U.st * 8, P.n, U.st, us);
 }
 
 // Background of one window (Poisson, clipped as draw_P_B_Tr does,
@@ -99,13 +105,18 @@ __device__ __forceinline__ int background(Rng &r, int navail, float lam_a, float
     return B[0];
 }
 
-// Photon mode: one dwell segment. Photons whose arrival offset falls in the
-// segment take its state; Poisson background then Binomial(signal, eps_state).
+// Photon mode: one dwell segment. Draw order per step: a fresh Philox block
+// [state, dwell, background A, background D], then (if the segment holds
+// photons) a fresh block for the binomial. Photons whose arrival offset falls
+// in the segment take its state; Poisson background, then Binomial(signal,
+// eps_state).
 __device__ __forceinline__ bool step_pho(Unit &U, const DevParams &P, const float *offs, float g,
                                          float ct, float r0, float bga, float bgd, int &lim,
                                          const float *inv) {
+    U.r.align();
+    const int st = next_state(U, P, U.r.u01());
+    U.st = st;
     float u = U.r.u01();
-    const int st = U.st;
     float tau = (P.kexit[st] > 0.0f) ? (-logf_(u)) * P.inv_kexit[st] : kInf;
     float tn = U.t + tau;
     bool cut = U.seg == kMaxSeg - 1;
@@ -118,35 +129,35 @@ __device__ __forceinline__ bool step_pho(Unit &U, const DevParams &P, const floa
     int nk = hi - U.lo;
     if (nk > 0) {
         int sig;
+        int ba = background(U.r, nk, bga * dt, bgd * dt, &sig, lim, inv);
+        U.r.align();
         if (P.V[st] > 0.0f) {
             float ek = eps_of(broaden(U.r, P.E[st], r0, P.V[st]), g, ct);
-            int ba = background(U.r, nk, bga * dt, bgd * dt, &sig, lim, inv);
             U.A += binom(U.r, sig, ek, lim, inv) + ba;
         } else {
-            int ba = background(U.r, nk, bga * dt, bgd * dt, &sig, lim, inv);
             U.A += binom_pre(U.r, sig, P.eps[st], P.bpp[st], P.blogq[st], P.brr[st], lim, inv) + ba;
         }
     }
     U.lo = hi;
     if (last) return true;
     U.t = tn;
-    U.st = jump_draw(P.jump_cdf + st * 8, P.n, st, U.r.u01());
     U.seg += 1;
     return false;
 }
 
-// Occupancy mode: one dwell segment; the last one also draws the background
-// and the single binomial split with the occupancy-weighted efficiency.
+// Occupancy mode: one dwell segment per step, draws [state, dwell]; after the
+// last one, a fresh block for the background and the single binomial split
+// with the occupancy-weighted efficiency.
 __device__ __forceinline__ bool step_occ(Unit &U, const DevParams &P, float g, float ct, float r0,
                                          float bga, float bgd, int &lim, const float *inv) {
-    bool last = true;
+    const int st = next_state(U, P, U.r.u01());
+    U.st = st;
     if (U.Tb > 0.0f) {
         float u = U.r.u01();
-        const int st = U.st;
         float tau = (P.kexit[st] > 0.0f) ? (-logf_(u)) * P.inv_kexit[st] : kInf;
         float tn = U.t + tau;
         bool cut = U.seg == kMaxSeg - 1;
-        last = !(tn < U.Tb) || cut;
+        bool last = !(tn < U.Tb) || cut;
         if (cut && tn < U.Tb) lim += 1;
         float dt = last ? U.Tb - U.t : tn - U.t;
         float es = P.E[st];
@@ -154,12 +165,12 @@ __device__ __forceinline__ bool step_occ(Unit &U, const DevParams &P, float g, f
         U.acc = fmaf(dt, es, U.acc);
         if (!last) {
             U.t = tn;
-            U.st = jump_draw(P.jump_cdf + st * 8, P.n, st, U.r.u01());
             U.seg += 1;
             return false;
         }
     }
-    float eeff = (U.Tb > 0.0f) ? U.acc / U.Tb : P.E[U.st];
+    float eeff = (U.Tb > 0.0f) ? U.acc / U.Tb : P.E[st];
+    U.r.align();
     int sig;
     int ba = background(U.r, U.Nb, bga * U.Tb, bgd * U.Tb, &sig, lim, inv);
     U.A = binom(U.r, sig, eps_of(eeff, g, ct), lim, inv) + ba;
@@ -244,7 +255,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) pda_kernel(const PdaArgs
         const uint32_t pw = a.pbase + (uint32_t)p;
         Unit U;
         bool active = tid < units;
-        if (active) unit_begin(U, sp, tid, a.S, tb0, sN, sT, a.seed, pw);
+        if (active) unit_begin(U, tid, a.S, tb0, sN, sT, a.seed, pw);
         while (__any_sync(0xffffffffu, active)) {
             bool fin = false;
             int bin = -1;
@@ -278,7 +289,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) pda_kernel(const PdaArgs
                 if (fin) {
                     const int u = base + __popc(need & lt_mask);
                     active = u < units;
-                    if (active) unit_begin(U, sp, u, a.S, tb0, sN, sT, a.seed, pw);
+                    if (active) unit_begin(U, u, a.S, tb0, sN, sT, a.seed, pw);
                 }
             }
         }

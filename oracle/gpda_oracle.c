@@ -56,6 +56,8 @@ static inline void rng_init(orc_rng *r, uint64_t seed, uint32_t pword, uint32_t 
     r->ctr[0] = 0; r->ctr[1] = s; r->ctr[2] = b; r->ctr[3] = pword;
     r->idx = 4;
 }
+/* the next draw starts a fresh block (the rest of the current one is dropped) */
+static inline void rng_align(orc_rng *r) { r->idx = 4; }
 static inline uint32_t rng_next(orc_rng *r) {
     if (r->idx == 4) {
         orc_philox4x32_10(r->ctr, r->key, r->buf);
