@@ -151,6 +151,28 @@ float gpda_kernel_ms(gpda_ctx *ctx);
 /* Number of units whose segment/rejection loops hit their bound so far. */
 int64_t gpda_limit_hits(gpda_ctx *ctx);
 
+/* No counterpart in the reference. For callers that cannot allocate device
+ * memory where they evaluate parameter sets (e.g. a framework whose caching
+ * allocator owns the device memory, or a loop that must not pay cudaMalloc's
+ * implicit synchronisation): runs the same Monte-Carlo kernel as
+ * gpda_run_batched over bursts [0,B) of caller-owned DEVICE arrays (N, T and,
+ * for photon mode, off_idx/offsets, laid out and valid as gpda_upload_bursts
+ * requires; not re-validated here) and writes P*nbins counts into the DEVICE
+ * array hist (zeroed first); with ohist/chi2 (device, nbins floats / P
+ * doubles) it also writes the reduced chi-square. params is a HOST array of
+ * P*n(n+1) floats. Allocates nothing: its scratch is a fixed array of about
+ * 73 KB inside the library, held by every device that loads it until exit,
+ * which limits P to 64 (GPDA_ERR_ARG beyond). Runs asynchronously on `stream`
+ * (a cudaStream_t, NULL = legacy default stream) on the current device.
+ * Calls share the scratch: calls that overlap on the GPU race and must be
+ * serialised by the caller. The first call on a device looks up the scratch
+ * address with that device current; make it before any stream capture. */
+int32_t gpda_run_pda_noalloc(const gpda_model *m, int32_t mode, int32_t P, int32_t n_states,
+                             const float *params, const int32_t *N, const float *T,
+                             const int64_t *off_idx, const float *offsets, int64_t B,
+                             int32_t samples, uint64_t seed, uint64_t *hist,
+                             const float *ohist, double *chi2, void *stream);
+
 /* ---------------------------------------------------------------- mc drop-in */
 
 typedef struct gpda_mc gpda_mc;
