@@ -19,8 +19,38 @@ namespace gpda {
 constexpr int kMaxStates = 8;
 constexpr int kMaxSeg = 65536;      // segments per unit before the trajectory is cut
 constexpr int kMaxRestart = 256;    // rejection restarts before the sampler gives up
+#ifndef GPDA_ALIGN_INLINE
+#define GPDA_ALIGN_INLINE 0
+#endif
 
 // ---------------------------------------------------------------- Philox
+// One Philox4x32-10 block for counter (c0, c1, c2, c3) under key (k0, k1).
+__device__ __forceinline__ uint4 philox_block_inline(uint32_t x0, uint32_t x1, uint32_t x2, uint32_t x3,
+                                                     uint32_t a, uint32_t b) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        uint64_t p0 = (uint64_t)0xD2511F53u * x0;
+        uint64_t p1 = (uint64_t)0xCD9E8D57u * x2;
+        uint32_t n0 = (uint32_t)(p1 >> 32) ^ x1 ^ a;
+        uint32_t n2 = (uint32_t)(p0 >> 32) ^ x3 ^ b;
+        x1 = (uint32_t)p1;
+        x3 = (uint32_t)p0;
+        x0 = n0;
+        x2 = n2;
+        a += 0x9E3779B9u;
+        b += 0xBB67AE85u;
+    }
+    return make_uint4(x0, x1, x2, x3);
+}
+
+// The same block behind one out-of-line copy: the draw sites of the samplers
+// call it instead of carrying their own inlined rounds, which keeps the
+// instruction footprint of the simulation loop small.
+__device__ __noinline__ uint4 philox_block(uint32_t x0, uint32_t x1, uint32_t x2, uint32_t x3,
+                                           uint32_t a, uint32_t b) {
+    return philox_block_inline(x0, x1, x2, x3, a, b);
+}
+
 struct Rng {
     uint32_t k0, k1, c1, c2, c3, blk;
     uint32_t w0, w1, w2, w3;
@@ -33,27 +63,13 @@ struct Rng {
         blk = 0u;
         idx = 4;
     }
-    __device__ __forceinline__ void block() {
-        uint32_t x0 = blk, x1 = c1, x2 = c2, x3 = c3;
-        uint32_t a = k0, b = k1;
-#pragma unroll
-        for (int r = 0; r < 10; ++r) {
-            uint64_t p0 = (uint64_t)0xD2511F53u * x0;
-            uint64_t p1 = (uint64_t)0xCD9E8D57u * x2;
-            uint32_t n0 = (uint32_t)(p1 >> 32) ^ x1 ^ a;
-            uint32_t n2 = (uint32_t)(p0 >> 32) ^ x3 ^ b;
-            x1 = (uint32_t)p1;
-            x3 = (uint32_t)p0;
-            x0 = n0;
-            x2 = n2;
-            a += 0x9E3779B9u;
-            b += 0xBB67AE85u;
-        }
-        w0 = x0; w1 = x1; w2 = x2; w3 = x3;
+    __device__ __forceinline__ void take(uint4 v) {
+        w0 = v.x; w1 = v.y; w2 = v.z; w3 = v.w;
         blk += 1u;
+        idx = 0;
     }
     __device__ __forceinline__ uint32_t next() {
-        if (idx == 4) { block(); idx = 0; }
+        if (idx == 4) take(philox_block(blk, c1, c2, c3, k0, k1));
         uint32_t r = (idx == 0) ? w0 : (idx == 1) ? w1 : (idx == 2) ? w2 : w3;
         ++idx;
         return r;
@@ -62,6 +78,15 @@ struct Rng {
     // discarded): keeps block generation at the same program point for all
     // lanes of a warp.
     __device__ __forceinline__ void align() { idx = 4; }
+    // align() + generate that block now, inline; only where at least one
+    // draw follows before the next align (same words as align()).
+    __device__ __forceinline__ void align_now() {
+#if GPDA_ALIGN_INLINE
+        take(philox_block_inline(blk, c1, c2, c3, k0, k1));
+#else
+        idx = 4;
+#endif
+    }
     // uniform on (0,1]: ((x >> 8) + 1) * 2^-24, exact
     __device__ __forceinline__ float u01() {
         return (float)((next() >> 8) + 1u) * 5.9604644775390625e-08f;

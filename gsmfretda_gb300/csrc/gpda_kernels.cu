@@ -113,7 +113,7 @@ __device__ __forceinline__ int background(Rng &r, int navail, float lam_a, float
 __device__ __forceinline__ bool step_pho(Unit &U, const DevParams &P, const float *offs, float g,
                                          float ct, float r0, float bga, float bgd, int &lim,
                                          const float *inv) {
-    U.r.align();
+    U.r.align_now();   // the state draw follows at once
     const int st = next_state(U, P, U.r.u01());
     U.st = st;
     float u = U.r.u01();
