@@ -59,6 +59,9 @@ struct gpda_ctx {
     unsigned long long *dLimit = nullptr;
     int32_t *dUnit = nullptr;
     size_t cap_unit = 0;
+    float *dCdf = nullptr;          // photon-mode binomial tables
+    uint16_t *dGuide = nullptr;
+    size_t cap_tab = 0;             // in (parameter set, state) tables
     // last launch
     int last_P = 0;
     bool last_chi2 = false;
@@ -162,12 +165,28 @@ int do_launch(gpda_ctx *c, int mode, int P, int n, const float *params, int64_t 
     const int nbins = c->model.nbins;
     CK(cudaMemcpyAsync(c->dParams, c->hParams, sizeof(DevParams) * P, cudaMemcpyHostToDevice, c->stream));
     CK(cudaEventRecord(c->params_ev, c->stream));
+    if (mode == GPDA_MODE_PHOTON) {
+        const size_t ntab = (size_t)P * n;
+        if (ntab > c->cap_tab) {
+            CK(cudaStreamSynchronize(c->stream));
+            free_dev(c->dCdf);
+            free_dev(c->dGuide);
+            c->dCdf = nullptr; c->dGuide = nullptr; c->cap_tab = 0;
+            CK(cudaMalloc(&c->dCdf, sizeof(float) * kTableRows * ntab));
+            CK(cudaMalloc(&c->dGuide, sizeof(uint16_t) * kTableRows * ntab));
+            c->cap_tab = ntab;
+        }
+        CK(launch_binom_tables(c->dParams, P, n, c->dCdf, c->dGuide, c->stream));
+        c->launches += 1;
+    }
     CK(cudaMemsetAsync(c->dHist, 0, sizeof(unsigned long long) * (size_t)P * nbins, c->stream));
     CK(cudaMemsetAsync(c->dWork, 0, sizeof(unsigned int), c->stream));
     c->last_P = P;
     c->last_chi2 = false;
     if (b1 == b0) return GPDA_OK;
     PdaArgs a{};
+    a.bcdf = c->dCdf;
+    a.bguide = c->dGuide;
     a.N = c->dN;
     a.T = c->dT;
     a.off_idx = c->dOffIdx;
@@ -277,6 +296,7 @@ void gpda_destroy(gpda_ctx *c) {
     free_dev(c->dN); free_dev(c->dT); free_dev(c->dOffIdx); free_dev(c->dOff);
     free_dev(c->dObs); free_dev(c->dParams); free_dev(c->dHist); free_dev(c->dChi2);
     free_dev(c->dWork); free_dev(c->dLimit); free_dev(c->dUnit); free_dev(c->dFlag);
+    free_dev(c->dCdf); free_dev(c->dGuide);
     if (c->hFlag) cudaFreeHost(c->hFlag);
     if (c->k0) cudaEventDestroy(c->k0);
     if (c->k1) cudaEventDestroy(c->k1);

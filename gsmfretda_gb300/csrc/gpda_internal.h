@@ -40,7 +40,19 @@ struct alignas(16) DevParams {
 static_assert(sizeof(DevParams) % 16 == 0, "DevParams must be 16-byte sized");
 constexpr int kParamWords = (int)(sizeof(DevParams) / 4);
 
+// Photon mode: Binomial(n, eps_s) for n <= kTableN (and V_s = 0) is drawn by
+// inversion of a float CDF row built per (parameter set, state, n); a guide
+// table of n+1 entries gives the starting index. Row (s, n) of parameter set
+// p starts at (p * n_states + s) * kTableRows + n (n + 1) / 2.
+#ifndef GPDA_TABLE_N
+#define GPDA_TABLE_N 255
+#endif
+constexpr int kTableN = GPDA_TABLE_N;
+constexpr int kTableRows = (kTableN + 1) * (kTableN + 2) / 2;   // entries per (parameter set, state)
+
 struct PdaArgs {
+    const float *bcdf;            // photon mode: CDF rows, P * n_states * kTableRows
+    const uint16_t *bguide;       // photon mode: guide rows, same indexing
     const int32_t *N;
     const float *T;
     const int64_t *off_idx;
@@ -86,6 +98,8 @@ cudaError_t launch_pda(int mode, const PdaArgs &a, int grid, size_t dyn_smem, cu
 cudaError_t launch_chi2(const unsigned long long *hist, const float *obs, int P, int nbins,
                         int left_pad, int S, int n_states, double *chi2, cudaStream_t st);
 cudaError_t launch_rc(const RcArgs &a, cudaStream_t st);
+cudaError_t launch_binom_tables(const DevParams *params, int P, int n_states, float *cdf,
+                                uint16_t *guide, cudaStream_t st);
 cudaError_t launch_validate(const int32_t *N, const float *T, const int64_t *off_idx,
                             const float *offsets, int64_t B, unsigned int *flag, int num_sms,
                             cudaStream_t st);

@@ -105,6 +105,29 @@ __device__ __forceinline__ int background(Rng &r, int navail, float lam_a, float
     return B[0];
 }
 
+// Binomial(n, eps) of a photon-mode segment (eps = eps_state, V_state = 0):
+// same early returns as binom(); for n <= kTableN one uniform inverts the
+// tabulated CDF of Binomial(n, min(eps, 1-eps)): the smallest k with
+// u <= cdf[k] (cdf[n] = 1); larger n fall back to BINV/BTRD.
+__device__ __forceinline__ int binom_table(Rng &r, int n, const DevParams &P, int st,
+                                           const float *cdf_p, const uint16_t *guide_p, int &lim,
+                                           const float *inv) {
+    const float p = P.eps[st];
+    if (n <= 0 || !(p > 0.0f)) return 0;
+    if (p >= 1.0f) return n;
+    if (n > kTableN) return binom_pre(r, n, p, P.bpp[st], P.blogq[st], P.brr[st], lim, inv);
+    const bool flip = p > 0.5f;
+    const int row = st * kTableRows + n * (n + 1) / 2;
+    const float *cdf = cdf_p + row;
+    const float u = r.u01();
+    int j = (int)(u * (float)(n + 1));
+    if (j > n) j = n;
+    int k = guide_p[row + j];
+    while (k > 0 && u <= __ldg(cdf + k - 1)) --k;
+    while (k < n && u > __ldg(cdf + k)) ++k;
+    return flip ? n - k : k;
+}
+
 // Photon mode: one dwell segment. Draw order per step: a fresh Philox block
 // [state, dwell, background A, background D], then (if the segment holds
 // photons) a fresh block for the binomial. Photons whose arrival offset falls
@@ -112,7 +135,8 @@ __device__ __forceinline__ int background(Rng &r, int navail, float lam_a, float
 // eps_state).
 __device__ __forceinline__ bool step_pho(Unit &U, const DevParams &P, const float *offs, float g,
                                          float ct, float r0, float bga, float bgd, int &lim,
-                                         const float *inv) {
+                                         const float *inv, const float *cdf_p,
+                                         const uint16_t *guide_p) {
     U.r.align_now();   // the state draw follows at once
     const int st = next_state(U, P, U.r.u01());
     U.st = st;
@@ -135,7 +159,7 @@ __device__ __forceinline__ bool step_pho(Unit &U, const DevParams &P, const floa
             float ek = eps_of(broaden(U.r, P.E[st], r0, P.V[st]), g, ct);
             U.A += binom(U.r, sig, ek, lim, inv) + ba;
         } else {
-            U.A += binom_pre(U.r, sig, P.eps[st], P.bpp[st], P.blogq[st], P.brr[st], lim, inv) + ba;
+            U.A += binom_table(U.r, sig, P, st, cdf_p, guide_p, lim, inv) + ba;
         }
     }
     U.lo = hi;
@@ -266,7 +290,9 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) pda_kernel(const PdaArgs
                         fin = step_occ(U, sp, a.gamma, a.ct, a.r0, a.bg_a, a.bg_d, lim, s_inv);
                     } else {
                         const float *offs = staged ? (s_ph + sOff[U.lb]) : (a.offsets + a.off_idx[tb0 + U.lb]);
-                        fin = step_pho(U, sp, offs, a.gamma, a.ct, a.r0, a.bg_a, a.bg_d, lim, s_inv);
+                        fin = step_pho(U, sp, offs, a.gamma, a.ct, a.r0, a.bg_a, a.bg_d, lim, s_inv,
+                                       a.bcdf + (size_t)p * sp.n * kTableRows,
+                                       a.bguide + (size_t)p * sp.n * kTableRows);
                     }
                 }
                 if (fin) {
@@ -453,6 +479,48 @@ __global__ void __launch_bounds__(kThreads) rc_kernel(const RcArgs a) {
     if (lim) atomicAdd(a.limit_hits, (unsigned long long)lim);
 }
 
+// ---------------------------------------------------------------- binomial tables
+
+// Row (p, s, n): cdf[k] = float(sum_{i<=k} C(n,i) pp^i qq^(n-i)) in FP64 with
+// pp = bpp[s] and qq = 1 - pp: pmf(0) = qq^n by repeated squaring, then
+// pmf(k) = (pmf(k-1) * ((n-k+1)/k)) * (pp/qq); values clamped to 1 and the
+// last entry set to 1. guide[j] = smallest k with cdf[k] >= j/(n+1) (float).
+// Every operation is an IEEE double op, so the host derives the same rows.
+__global__ void binom_table_kernel(const DevParams *params, int P, int n_states, float *cdf_all,
+                                   uint16_t *guide_all) {
+    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t total = (int64_t)P * n_states * (kTableN + 1);
+    if (tid >= total) return;
+    const int nn = (int)(tid % (kTableN + 1));
+    const int s = (int)((tid / (kTableN + 1)) % n_states);
+    const int p = (int)(tid / ((int64_t)(kTableN + 1) * n_states));
+    const size_t row = ((size_t)p * n_states + s) * kTableRows + (size_t)nn * (nn + 1) / 2;
+    float *cdf = cdf_all + row;
+    uint16_t *guide = guide_all + row;
+    const double pp = (double)params[p].bpp[s];
+    const double qq = 1.0 - pp;
+    const double ratio = pp / qq;
+    double f = 1.0, base = qq;
+    for (int e = nn; e > 0; e >>= 1) {
+        if (e & 1) f = f * base;
+        base = base * base;
+    }
+    double cum = 0.0;
+    for (int k = 0; k <= nn; ++k) {
+        if (k > 0) f = (f * ((double)(nn - k + 1) / (double)k)) * ratio;
+        cum = cum + f;
+        float c = (float)cum;
+        cdf[k] = c < 1.0f ? c : 1.0f;
+    }
+    cdf[nn] = 1.0f;
+    int k = 0;
+    for (int j = 0; j <= nn; ++j) {
+        const float thr = (float)j / (float)(nn + 1);
+        while (k < nn && cdf[k] < thr) ++k;
+        guide[j] = (uint16_t)k;
+    }
+}
+
 // ---------------------------------------------------------------- burst-store validation
 
 // One warp per burst: photon counts in range, durations finite and >= 0,
@@ -487,6 +555,14 @@ __global__ void validate_kernel(const int32_t *N, const float *T, const int64_t 
 }
 
 // ---------------------------------------------------------------- launchers
+
+cudaError_t launch_binom_tables(const DevParams *params, int P, int n_states, float *cdf,
+                                uint16_t *guide, cudaStream_t st) {
+    const int64_t total = (int64_t)P * n_states * (kTableN + 1);
+    if (total <= 0) return cudaSuccess;
+    binom_table_kernel<<<(unsigned)((total + 127) / 128), 128, 0, st>>>(params, P, n_states, cdf, guide);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_validate(const int32_t *N, const float *T, const int64_t *off_idx,
                             const float *offsets, int64_t B, unsigned int *flag, int num_sms,

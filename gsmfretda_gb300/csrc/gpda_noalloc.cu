@@ -12,8 +12,10 @@
 // loop-limit counter) lives in one fixed array inside this library.
 //
 // The array is a file-scope __device__ array of kNoAllocScratchBytes bytes
-// (about 73 KB): every device that loads the library holds a copy until the
-// process exits. It limits a call to kNoAllocMaxP (64) parameter sets.
+// (about 1.7 MB): every device that loads the library holds a copy until the
+// process exits. It limits a call to kNoAllocMaxP (64) parameter sets, and in
+// photon mode to kNoAllocMaxTables (8) parameter-set x state binomial tables
+// (P * n_states <= 8).
 // All calls share it and it keeps the last call's contents; the counters are
 // cleared on every call, but calls whose work overlaps on the GPU (different
 // streams, or different host threads without ordering between them) race on
@@ -35,6 +37,7 @@ using namespace gpda;
 namespace {
 
 constexpr int kNoAllocMaxP = 64;
+constexpr int kNoAllocMaxTables = 8;   // photon mode: P * n_states (parameter set, state) tables
 constexpr int kNoAllocMaxDevices = 64;
 
 struct NoAllocScratch {
@@ -42,6 +45,8 @@ struct NoAllocScratch {
     unsigned int work;
     unsigned int pad_[3];
     unsigned long long limit_hits;
+    float cdf[kNoAllocMaxTables * kTableRows];
+    uint16_t guide[kNoAllocMaxTables * kTableRows];
 };
 constexpr size_t kNoAllocScratchBytes = sizeof(NoAllocScratch);
 
@@ -96,6 +101,7 @@ extern "C" int32_t gpda_run_pda_noalloc(const gpda_model *m, int32_t mode, int32
     if (n_states < 1 || n_states > GPDA_MAX_STATES || samples < 1 || !params) return GPDA_ERR_ARG;
     if (!N || !T || !hist || B < 1 || B * (int64_t)samples > (int64_t)INT32_MAX) return GPDA_ERR_ARG;
     if (mode == GPDA_MODE_PHOTON && (!off_idx || !offsets)) return GPDA_ERR_ARG;
+    if (mode == GPDA_MODE_PHOTON && P * n_states > kNoAllocMaxTables) return GPDA_ERR_ARG;
     if ((ohist == nullptr) != (chi2 == nullptr)) return GPDA_ERR_ARG;
     if (mm.nbins < 1 || mm.nbins > GPDA_MAX_BINS || mm.left_pad < 0 || mm.left_pad > mm.nbins ||
         !(mm.gamma > 0.0f) || !(mm.crosstalk >= 0.0f) || !(mm.bg_a >= 0.0f) || !(mm.bg_d >= 0.0f) ||
@@ -129,7 +135,12 @@ extern "C" int32_t gpda_run_pda_noalloc(const gpda_model *m, int32_t mode, int32
         cudaGetLastError();
         return GPDA_ERR_CUDA;
     }
+    if (mode == GPDA_MODE_PHOTON &&
+        launch_binom_tables(sc->params, P, n_states, sc->cdf, sc->guide, st) != cudaSuccess)
+        return GPDA_ERR_CUDA;
     PdaArgs a{};
+    a.bcdf = sc->cdf;
+    a.bguide = sc->guide;
     a.N = N;
     a.T = T;
     a.off_idx = off_idx;

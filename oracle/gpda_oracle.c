@@ -322,6 +322,30 @@ static inline int ref_bin_d(double z, int nbins) {
 static float inv_tab_f[64];
 static double inv_tab_d[64];
 
+/* photon mode: Binomial(n, eps_s) with n <= ORC_TABLE_N (and V_s = 0) is
+ * drawn by inverting a tabulated CDF (one uniform) */
+#define ORC_TABLE_N 255
+#define ORC_TABLE_ROWS ((ORC_TABLE_N + 1) * (ORC_TABLE_N + 2) / 2)
+
+/* CDF row of Binomial(nn, pp) in double: pmf(0) = qq^nn by repeated squaring,
+ * pmf(k) = (pmf(k-1) * ((nn-k+1)/k)) * (pp/qq), running sum clamped to 1,
+ * last entry 1. */
+static void binom_cdf_row(double pp, int nn, double *out) {
+    double qq = 1.0 - pp;
+    double ratio = pp / qq;
+    double f = 1.0, base = qq;
+    for (int e = nn; e > 0; e >>= 1) {
+        if (e & 1) f = f * base;
+        base = base * base;
+    }
+    double cum = 0.0;
+    for (int k = 0; k <= nn; ++k) {
+        if (k > 0) f = (f * ((double)(nn - k + 1) / (double)k)) * ratio;
+        cum = cum + f;
+        out[k] = cum;
+    }
+}
+
 #define ORC_MAX_SEG 65536
 #define ORC_MAX_RESTART 256
 

@@ -20,7 +20,7 @@ def test_noalloc_matches_batched_on_two_calls(gpda_lib):
 
     bs, n, args1, md, _ = synth.photon_3state(B=3000, seed=71)
     S = 16
-    P = 3
+    P = 2                       # photon mode: P * n_states <= 8 binomial tables
     rng = np.random.default_rng(72)
     params = np.concatenate([synth.random_3state_args(rng) for _ in range(P)]).astype(np.float32)
     nb = md["nbins"]
