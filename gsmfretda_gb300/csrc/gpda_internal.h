@@ -45,7 +45,7 @@ constexpr int kParamWords = (int)(sizeof(DevParams) / 4);
 // table of n+1 entries gives the starting index. Row (s, n) of parameter set
 // p starts at (p * n_states + s) * kTableRows + n (n + 1) / 2.
 #ifndef GPDA_TABLE_N
-#define GPDA_TABLE_N 255
+#define GPDA_TABLE_N 511
 #endif
 constexpr int kTableN = GPDA_TABLE_N;
 constexpr int kTableRows = (kTableN + 1) * (kTableN + 2) / 2;   // entries per (parameter set, state)

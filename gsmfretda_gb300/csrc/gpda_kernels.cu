@@ -483,15 +483,21 @@ __global__ void __launch_bounds__(kThreads) rc_kernel(const RcArgs a) {
 
 // Row (p, s, n): cdf[k] = float(sum_{i<=k} C(n,i) pp^i qq^(n-i)) in FP64 with
 // pp = bpp[s] and qq = 1 - pp: pmf(0) = qq^n by repeated squaring, then
-// pmf(k) = (pmf(k-1) * ((n-k+1)/k)) * (pp/qq); values clamped to 1 and the
-// last entry set to 1. guide[j] = smallest k with cdf[k] >= j/(n+1) (float).
-// Every operation is an IEEE double op, so the host derives the same rows.
+// pmf(k) = ((pmf(k-1) * (n-k+1)) * inv[k]) * (pp/qq) with inv[k] = 1.0/k;
+// values clamped to 1 and the last entry set to 1. guide[j] = smallest k with
+// cdf[k] >= j/(n+1) (float). Every operation is an IEEE double op, so the
+// host derives the same rows. One thread per row, 32-thread blocks so that
+// the rows spread over many SMs (FP64 throughput per SM is low).
 __global__ void binom_table_kernel(const DevParams *params, int P, int n_states, float *cdf_all,
                                    uint16_t *guide_all) {
+    __shared__ double s_inv[kTableN + 1];
+    for (int k = threadIdx.x; k <= kTableN; k += blockDim.x) s_inv[k] = k > 0 ? 1.0 / (double)k : 0.0;
+    __syncthreads();
     const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t total = (int64_t)P * n_states * (kTableN + 1);
     if (tid >= total) return;
-    const int nn = (int)(tid % (kTableN + 1));
+    // longest rows first across blocks: row length is nn + 1
+    const int nn = kTableN - (int)(tid % (kTableN + 1));
     const int s = (int)((tid / (kTableN + 1)) % n_states);
     const int p = (int)(tid / ((int64_t)(kTableN + 1) * n_states));
     const size_t row = ((size_t)p * n_states + s) * kTableRows + (size_t)nn * (nn + 1) / 2;
@@ -507,7 +513,7 @@ __global__ void binom_table_kernel(const DevParams *params, int P, int n_states,
     }
     double cum = 0.0;
     for (int k = 0; k <= nn; ++k) {
-        if (k > 0) f = (f * ((double)(nn - k + 1) / (double)k)) * ratio;
+        if (k > 0) f = ((f * (double)(nn - k + 1)) * s_inv[k]) * ratio;
         cum = cum + f;
         float c = (float)cum;
         cdf[k] = c < 1.0f ? c : 1.0f;
@@ -560,7 +566,7 @@ cudaError_t launch_binom_tables(const DevParams *params, int P, int n_states, fl
                                 uint16_t *guide, cudaStream_t st) {
     const int64_t total = (int64_t)P * n_states * (kTableN + 1);
     if (total <= 0) return cudaSuccess;
-    binom_table_kernel<<<(unsigned)((total + 127) / 128), 128, 0, st>>>(params, P, n_states, cdf, guide);
+    binom_table_kernel<<<(unsigned)((total + 31) / 32), 32, 0, st>>>(params, P, n_states, cdf, guide);
     return cudaGetLastError();
 }
 

@@ -12,7 +12,7 @@
 // loop-limit counter) lives in one fixed array inside this library.
 //
 // The array is a file-scope __device__ array of kNoAllocScratchBytes bytes
-// (about 1.7 MB): every device that loads the library holds a copy until the
+// (about 6.4 MB): every device that loads the library holds a copy until the
 // process exits. It limits a call to kNoAllocMaxP (64) parameter sets, and in
 // photon mode to kNoAllocMaxTables (8) parameter-set x state binomial tables
 // (P * n_states <= 8).

@@ -161,8 +161,9 @@ int64_t gpda_limit_hits(gpda_ctx *ctx);
  * array hist (zeroed first); with ohist/chi2 (device, nbins floats / P
  * doubles) it also writes the reduced chi-square. params is a HOST array of
  * P*n(n+1) floats. Allocates nothing: its scratch is a fixed array of about
- * 73 KB inside the library, held by every device that loads it until exit,
- * which limits P to 64 (GPDA_ERR_ARG beyond). Runs asynchronously on `stream`
+ * 6.4 MB inside the library, held by every device that loads it until exit,
+ * which limits P to 64, and in photon mode P*n_states to 8 (GPDA_ERR_ARG
+ * beyond). Runs asynchronously on `stream`
  * (a cudaStream_t, NULL = legacy default stream) on the current device.
  * Calls share the scratch: calls that overlap on the GPU race and must be
  * serialised by the caller. The first call on a device looks up the scratch

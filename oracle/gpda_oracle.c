@@ -324,12 +324,12 @@ static double inv_tab_d[64];
 
 /* photon mode: Binomial(n, eps_s) with n <= ORC_TABLE_N (and V_s = 0) is
  * drawn by inverting a tabulated CDF (one uniform) */
-#define ORC_TABLE_N 255
+#define ORC_TABLE_N 511
 #define ORC_TABLE_ROWS ((ORC_TABLE_N + 1) * (ORC_TABLE_N + 2) / 2)
 
 /* CDF row of Binomial(nn, pp) in double: pmf(0) = qq^nn by repeated squaring,
- * pmf(k) = (pmf(k-1) * ((nn-k+1)/k)) * (pp/qq), running sum clamped to 1,
- * last entry 1. */
+ * pmf(k) = ((pmf(k-1) * (nn-k+1)) * (1/k)) * (pp/qq), running sum clamped to
+ * 1, last entry 1. */
 static void binom_cdf_row(double pp, int nn, double *out) {
     double qq = 1.0 - pp;
     double ratio = pp / qq;
@@ -340,7 +340,7 @@ static void binom_cdf_row(double pp, int nn, double *out) {
     }
     double cum = 0.0;
     for (int k = 0; k <= nn; ++k) {
-        if (k > 0) f = (f * ((double)(nn - k + 1) / (double)k)) * ratio;
+        if (k > 0) f = ((f * (double)(nn - k + 1)) * (1.0 / (double)k)) * ratio;
         cum = cum + f;
         out[k] = cum;
     }
