@@ -481,50 +481,110 @@ __global__ void __launch_bounds__(kThreads) rc_kernel(const RcArgs a) {
 
 // ---------------------------------------------------------------- binomial tables
 
-// Row (p, s, n): cdf[k] = float(sum_{i<=k} C(n,i) pp^i qq^(n-i)) in FP64 with
-// pp = bpp[s] and qq = 1 - pp: pmf(0) = qq^n by repeated squaring, then
-// pmf(k) = ((pmf(k-1) * (n-k+1)) * inv[k]) * (pp/qq) with inv[k] = 1.0/k;
-// values clamped to 1 and the last entry set to 1. guide[j] = smallest k with
-// cdf[k] >= j/(n+1) (float). Every operation is an IEEE double op, so the
-// host derives the same rows. One thread per row, 32-thread blocks so that
-// the rows spread over many SMs (FP64 throughput per SM is low).
+// Double-float arithmetic (a value is hi + lo, two FP32 numbers): error-free
+// products by fmaf and error-free sums (Dekker, Knuth), about 44 significant
+// bits. GB300 runs FP64 at a small fraction of its FP32 rate, so the tables are
+// built on the FP32 pipes. Every step is an IEEE FP32 operation or fmaf, in a
+// fixed order, so the host reproduces the rows bit for bit.
+struct DF {
+    float hi, lo;
+};
+__device__ __forceinline__ DF df_fast_sum(float a, float b) {   // |a| >= |b|
+    float s = a + b;
+    return {s, b - (s - a)};
+}
+__device__ __forceinline__ DF df_mul(DF a, DF b) {
+    float p = a.hi * b.hi;
+    float e = fmaf(a.hi, b.hi, -p);
+    e = fmaf(a.hi, b.lo, e);
+    e = fmaf(a.lo, b.hi, e);
+    return df_fast_sum(p, e);
+}
+__device__ __forceinline__ DF df_add(DF a, DF b) {
+    float s = a.hi + b.hi;
+    float bb = s - a.hi;
+    float e = (a.hi - (s - bb)) + (b.hi - bb);
+    e = e + (a.lo + b.lo);
+    return df_fast_sum(s, e);
+}
+// x / y for float x, y > 0: one correction step
+__device__ __forceinline__ DF df_div(float x, DF y) {
+    float q = x / y.hi;
+    DF qy = df_mul({q, 0.0f}, y);
+    float r = (x - qy.hi) - qy.lo;
+    return df_fast_sum(q, r / y.hi);
+}
+// x / y for double-float x, y > 0
+__device__ __forceinline__ DF df_div2(DF x, DF y) {
+    float q = x.hi / y.hi;
+    DF qy = df_mul({q, 0.0f}, y);
+    DF rem = df_add(x, {-qy.hi, -qy.lo});
+    return df_fast_sum(q, rem.hi / y.hi);
+}
+// 1/k as a double-float, k >= 1
+__device__ __forceinline__ DF df_recip(int k) {
+    const float kf = (float)k;
+    const float ih = 1.0f / kf;
+    return df_fast_sum(ih, fmaf(-ih, kf, 1.0f) / kf);
+}
+
+// Row (p, s, n) of the photon-mode binomial tables, pp = bpp[s] <= 1/2,
+// qq = 1 - pp, all in double-float: relative probabilities w(k) = pmf(k) /
+// pmf(m) around the mode m = min(floor((n+1) pp), n), upward w(k) =
+// w(k-1) * ((n-k+1) / k) * (pp/qq), downward w(k) = w(k+1) * ((k+1) / (n-k)) *
+// (qq/pp) (far tails underflow harmlessly to 0; FP32 cannot hold qq^n), the
+// total W summed upward then downward, then cdf[k] = float((sum_{i<=k} w(i)) *
+// (1/W)) clamped to 1 with cdf[n] = 1. guide[j] is the first k with
+// cdf[k] >= j/(n+1) (approximately; the draw corrects any start index).
+// One thread per row, 32-thread blocks so the rows spread over many SMs;
+// longest rows first.
 __global__ void binom_table_kernel(const DevParams *params, int P, int n_states, float *cdf_all,
                                    uint16_t *guide_all) {
-    __shared__ double s_inv[kTableN + 1];
-    for (int k = threadIdx.x; k <= kTableN; k += blockDim.x) s_inv[k] = k > 0 ? 1.0 / (double)k : 0.0;
-    __syncthreads();
     const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t total = (int64_t)P * n_states * (kTableN + 1);
     if (tid >= total) return;
-    // longest rows first across blocks: row length is nn + 1
     const int nn = kTableN - (int)(tid % (kTableN + 1));
     const int s = (int)((tid / (kTableN + 1)) % n_states);
     const int p = (int)(tid / ((int64_t)(kTableN + 1) * n_states));
     const size_t row = ((size_t)p * n_states + s) * kTableRows + (size_t)nn * (nn + 1) / 2;
     float *cdf = cdf_all + row;
     uint16_t *guide = guide_all + row;
-    const double pp = (double)params[p].bpp[s];
-    const double qq = 1.0 - pp;
-    const double ratio = pp / qq;
-    double f = 1.0, base = qq;
-    for (int e = nn; e > 0; e >>= 1) {
-        if (e & 1) f = f * base;
-        base = base * base;
+    const float pp = params[p].bpp[s];
+    const DF qq = df_fast_sum(1.0f, -pp);
+    const DF up = df_div(pp, qq);
+    const DF down = df_div2(qq, {pp, 0.0f});
+    int m = (int)floorf((float)(nn + 1) * pp);
+    if (m > nn) m = nn;
+    DF W = {1.0f, 0.0f};
+    cdf[m] = 1.0f;
+    DF w = {1.0f, 0.0f};
+#pragma unroll 4
+    for (int k = m + 1; k <= nn; ++k) {
+        w = df_mul(w, df_mul(df_mul({(float)(nn - k + 1), 0.0f}, df_recip(k)), up));
+        cdf[k] = w.hi + w.lo;
+        W = df_add(W, w);
     }
-    double cum = 0.0;
+    w = {1.0f, 0.0f};
+#pragma unroll 4
+    for (int k = m - 1; k >= 0; --k) {
+        w = df_mul(w, df_mul(df_mul({(float)(k + 1), 0.0f}, df_recip(nn - k)), down));
+        cdf[k] = w.hi + w.lo;
+        W = df_add(W, w);
+    }
+    const DF invW = df_div(1.0f, W);
+    const float gstep = 1.0f / (float)(nn + 1);
+    int j = 0;
+    DF cum = {0.0f, 0.0f};
+#pragma unroll 4
     for (int k = 0; k <= nn; ++k) {
-        if (k > 0) f = ((f * (double)(nn - k + 1)) * s_inv[k]) * ratio;
-        cum = cum + f;
-        float c = (float)cum;
-        cdf[k] = c < 1.0f ? c : 1.0f;
+        cum = df_add(cum, {cdf[k], 0.0f});
+        DF v = df_mul(cum, invW);
+        float c = v.hi + v.lo;
+        c = (k == nn) ? 1.0f : (c < 1.0f ? c : 1.0f);
+        cdf[k] = c;
+        while (j <= nn && (float)j * gstep <= c) guide[j++] = (uint16_t)k;
     }
-    cdf[nn] = 1.0f;
-    int k = 0;
-    for (int j = 0; j <= nn; ++j) {
-        const float thr = (float)j / (float)(nn + 1);
-        while (k < nn && cdf[k] < thr) ++k;
-        guide[j] = (uint16_t)k;
-    }
+    while (j <= nn) guide[j++] = (uint16_t)nn;
 }
 
 // ---------------------------------------------------------------- burst-store validation

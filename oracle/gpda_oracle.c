@@ -327,10 +327,87 @@ static double inv_tab_d[64];
 #define ORC_TABLE_N 511
 #define ORC_TABLE_ROWS ((ORC_TABLE_N + 1) * (ORC_TABLE_N + 2) / 2)
 
-/* CDF row of Binomial(nn, pp) in double: pmf(0) = qq^nn by repeated squaring,
- * pmf(k) = ((pmf(k-1) * (nn-k+1)) * (1/k)) * (pp/qq), running sum clamped to
- * 1, last entry 1. */
-static void binom_cdf_row(double pp, int nn, double *out) {
+/* Double-float arithmetic (hi + lo in two floats; Dekker/Knuth error-free
+ * transformations with fmaf), as the device builds its binomial tables. */
+typedef struct { float hi, lo; } orc_df;
+static inline orc_df df_fast_sum(float a, float b) {
+    float s = a + b;
+    orc_df r = {s, b - (s - a)};
+    return r;
+}
+static inline orc_df df_mul(orc_df a, orc_df b) {
+    float p = a.hi * b.hi;
+    float e = fmaf(a.hi, b.hi, -p);
+    e = fmaf(a.hi, b.lo, e);
+    e = fmaf(a.lo, b.hi, e);
+    return df_fast_sum(p, e);
+}
+static inline orc_df df_add(orc_df a, orc_df b) {
+    float s = a.hi + b.hi;
+    float bb = s - a.hi;
+    float e = (a.hi - (s - bb)) + (b.hi - bb);
+    e = e + (a.lo + b.lo);
+    return df_fast_sum(s, e);
+}
+static inline orc_df df_div(float x, orc_df y) {
+    float q = x / y.hi;
+    orc_df qf = {q, 0.0f};
+    orc_df qy = df_mul(qf, y);
+    float r = (x - qy.hi) - qy.lo;
+    return df_fast_sum(q, r / y.hi);
+}
+static inline orc_df df_div2(orc_df x, orc_df y) {
+    float q = x.hi / y.hi;
+    orc_df qf = {q, 0.0f};
+    orc_df qy = df_mul(qf, y);
+    orc_df nqy = {-qy.hi, -qy.lo};
+    orc_df rem = df_add(x, nqy);
+    return df_fast_sum(q, rem.hi / y.hi);
+}
+static inline orc_df df_recip(int k) {
+    float kf = (float)k;
+    float ih = 1.0f / kf;
+    return df_fast_sum(ih, fmaf(-ih, kf, 1.0f) / kf);
+}
+
+/* CDF row of Binomial(nn, pp), pp <= 1/2, in double-float around the mode
+ * (relative probabilities from w(m) = 1 upward then downward, total, running
+ * sum times 1/total), clamped to 1 with out[nn] = 1, as the device builds it. */
+static void binom_cdf_row_df(float pp, int nn, float *out) {
+    orc_df qq = df_fast_sum(1.0f, -pp);
+    orc_df up = df_div(pp, qq);
+    orc_df ppd = {pp, 0.0f};
+    orc_df down = df_div2(qq, ppd);
+    int m = (int)floorf((float)(nn + 1) * pp);
+    if (m > nn) m = nn;
+    orc_df W = {1.0f, 0.0f}, w = {1.0f, 0.0f};
+    out[m] = 1.0f;
+    for (int k = m + 1; k <= nn; ++k) {
+        orc_df a = {(float)(nn - k + 1), 0.0f};
+        w = df_mul(w, df_mul(df_mul(a, df_recip(k)), up));
+        out[k] = w.hi + w.lo;
+        W = df_add(W, w);
+    }
+    w.hi = 1.0f; w.lo = 0.0f;
+    for (int k = m - 1; k >= 0; --k) {
+        orc_df a = {(float)(k + 1), 0.0f};
+        w = df_mul(w, df_mul(df_mul(a, df_recip(nn - k)), down));
+        out[k] = w.hi + w.lo;
+        W = df_add(W, w);
+    }
+    orc_df invW = df_div(1.0f, W);
+    orc_df cum = {0.0f, 0.0f};
+    for (int k = 0; k <= nn; ++k) {
+        orc_df t = {out[k], 0.0f};
+        cum = df_add(cum, t);
+        orc_df v = df_mul(cum, invW);
+        float c = v.hi + v.lo;
+        out[k] = (k == nn) ? 1.0f : (c < 1.0f ? c : 1.0f);
+    }
+}
+
+/* the FP64 transcription's rows: the same recurrence in double */
+static void binom_cdf_row_d(double pp, int nn, double *out) {
     double qq = 1.0 - pp;
     double ratio = pp / qq;
     double f = 1.0, base = qq;
@@ -340,7 +417,7 @@ static void binom_cdf_row(double pp, int nn, double *out) {
     }
     double cum = 0.0;
     for (int k = 0; k <= nn; ++k) {
-        if (k > 0) f = ((f * (double)(nn - k + 1)) * (1.0 / (double)k)) * ratio;
+        if (k > 0) f = f * (((double)(nn - k + 1) * (1.0 / (double)k)) * ratio);
         cum = cum + f;
         out[k] = cum;
     }
@@ -415,6 +492,8 @@ static void init_lf_d(void) {
 }
 
 /* ------------------------------------------------------------------ */
+void orc_binom_cdf_row(float pp, int32_t nn, float *out) { binom_cdf_row_df(pp, nn, out); }
+
 int orc_build_params(int32_t n, const float *args, const orc_model *m, orc_params *out) {
     (void)m;
     orc_derived d;

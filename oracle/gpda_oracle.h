@@ -116,6 +116,9 @@ int orc_sample(int kind, uint64_t seed, int32_t n, float p, int64_t count, doubl
 int orc_sample_cat(uint64_t seed, int32_t mode, int32_t n, const float *w, int32_t from,
                    int64_t count, int32_t *out);
 
+/* photon-mode binomial table row: cdf of Binomial(nn, pp), pp <= 1/2 */
+void orc_binom_cdf_row(float pp, int32_t nn, float *out);
+
 /* host-side parameter derivation (pda + ref-compat tables) */
 int orc_build_params(int32_t n, const float *args, const orc_model *m, orc_params *out);
 

@@ -63,6 +63,7 @@ def lib():
         _lib.orc_sample.argtypes = [C.c_int, C.c_uint64, C.c_int32, C.c_float, C.c_int64, C.c_void_p]
         _lib.orc_sample_cat.argtypes = [C.c_uint64, C.c_int32, C.c_int32, C.c_void_p, C.c_int32,
                                         C.c_int64, C.c_void_p]
+        _lib.orc_binom_cdf_row.argtypes = [C.c_float, C.c_int32, C.c_void_p]
         _lib.orc_build_params.argtypes = [C.c_int32, C.c_void_p, C.POINTER(OrcModel), C.POINTER(OrcParams)]
         _lib.orc_run_pda.argtypes = [C.POINTER(OrcBursts), C.c_int32, C.c_void_p, C.c_int32,
                                      C.POINTER(OrcModel), C.c_int32, C.c_int32, C.c_uint64,
@@ -110,6 +111,12 @@ def sample_cat(seed, mode, w, count, frm=0, n=None):
     rc = lib().orc_sample_cat(seed, mode, n, _ptr(w), frm, count, _ptr(out))
     if rc != 0:
         raise ValueError(rc)
+    return out
+
+
+def binom_cdf_row(pp, nn):
+    out = np.zeros(nn + 1, dtype=np.float32)
+    lib().orc_binom_cdf_row(pp, nn, _ptr(out))
     return out
 
 

@@ -185,3 +185,16 @@ def test_fp32_and_fp64_samplers_make_the_same_decisions(orc):
         a = orc.sample(kind32, 81, n, p, 50_000)
         b = orc.sample(kind64, 81, n, p, 50_000)
         assert (a != b).mean() < 1e-3
+
+
+@pytest.mark.parametrize("pp", [0.5, 0.49, 0.24, 0.15, 0.05, 0.013, 1e-4])
+def test_binomial_table_rows_match_exact_cdf(orc, pp):
+    """Photon-mode binomial tables (double-float rows around the mode) against
+    the exact CDF, for every n up to the table bound."""
+    worst = 0.0
+    for nn in list(range(0, 40)) + [63, 100, 127, 128, 255, 256, 300, 511]:
+        row = orc.binom_cdf_row(pp, nn)
+        exact = stats.binom.cdf(np.arange(nn + 1), nn, np.float64(np.float32(pp)))
+        assert row[-1] == 1.0 and np.all(np.diff(row) >= 0)
+        worst = max(worst, np.abs(row - exact).max())
+    assert worst < 5e-7
