@@ -38,9 +38,14 @@ WORKLOAD = "photon_3state"
 B_FULL = 100_000
 SAMPLES = 100
 HELD_OUT_SEED = 0x0B5E
-# fixed cost model per unit of this workload (ALU ops): 25 per Philox word,
-# 16 per log, 40 per BTRD-class binomial, 2 per photon compare
-ALU_OPS_PER_UNIT = 1040.0
+# Thread instructions per unit of this workload, from ncu (warp instructions x
+# active threads per instruction / units; profiles/pda_kernel_photon_3state.txt);
+# the fixed cost model (25 per Philox word, 16 per log, 40 per binomial, 2 per
+# photon compare) gives 1,040.
+ALU_OPS_PER_UNIT = 1168.0
+# DRAM bytes (read + write) of one MC launch on this workload, from the same
+# ncu capture; the algorithmic figure is computed live below.
+NCU_TRAFFIC_BYTES = 63.41e6
 
 
 def parse():
@@ -115,6 +120,18 @@ class ClockSampler:
                 "sm_max_mhz": max(smax) if smax else None,
                 "reasons": reasons, "samples_in_timed_region": len(inside),
                 "power_w_max": max((num(s[3]) or 0.0) for s in inside)}
+
+
+def max_over_ranks(x, dist, device=None):
+    """Largest value of x over all ranks (all_reduce MAX); x itself without a
+    process group. Replicas time their own copy of the workload; the job's
+    time is the slowest rank's."""
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
 
 
 def workload(B):
@@ -336,10 +353,7 @@ def main():
     hist, chi2 = eng.fetch(1)
     time.sleep(0.2)
     clocks.stop()
-    if dist:
-        t = torch.tensor([total_s], device=f"cuda:{local}", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_s = float(t.item())
+    total_s = max_over_ranks(total_s, dist, device=f"cuda:{local}")
     value = world * units * a.steps / total_s
 
     # ---------------- end to end through the C ABI with pinned host buffers
@@ -358,11 +372,7 @@ def main():
         t1 = time.perf_counter()
         if k >= 2:
             e2e_s.append(t1 - t0)
-    e2e_mean = sum(e2e_s) / len(e2e_s)
-    if dist:
-        t = torch.tensor([e2e_mean], device=f"cuda:{local}", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_mean = float(t.item())
+    e2e_mean = max_over_ranks(sum(e2e_s) / len(e2e_s), dist, device=f"cuda:{local}")
     h2d = hN.nbytes + hT.nbytes + hOI.nbytes + hOF.nbytes + hA.nbytes
     d2h = 8 * md["nbins"] + 8 + 4
 
@@ -387,10 +397,12 @@ def main():
         "gpu_launches": int(launches),
         "clocks": clocks.summary(),
         "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved_gbs / hbm_peak, "traffic": None, "peak_kind": peak_kind,
+                     "frac": achieved_gbs / hbm_peak,
+                     "traffic": NCU_TRAFFIC_BYTES if bs.B == B_FULL else None, "peak_kind": peak_kind,
                      "algorithmic_bytes_per_launch": alg_bytes, "kernel_ms": kavg_ms,
-                     "alu": {"achieved": alu_achieved, "peak": alu_peak, "unit": "Gop/s",
-                             "frac": alu_achieved / alu_peak, "ops_per_unit": ALU_OPS_PER_UNIT}},
+                     "alu": {"achieved": alu_achieved, "peak": alu_peak, "unit": "Ginst/s",
+                             "frac": alu_achieved / alu_peak, "inst_per_unit": ALU_OPS_PER_UNIT,
+                             "what": "thread-instruction issue rate vs 152 SMs x 128 lanes x SM clock"}},
         "chi2_last": float(chi2[0]),
     }
     if rank == 0 and world == 1 and not a.no_cpu_baseline:
