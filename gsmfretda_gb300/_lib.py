@@ -57,6 +57,9 @@ SIGNATURES = {
     "gpda_launch_count": (_I64, [_VP]),
     "gpda_limit_hits": (_I64, [_VP]),
     "gpda_kernel_ms": (_F, [_VP]),
+    "gpda_expected_hist": (_I32, [_VP, _I32, _I32, _VP, _VP, _I32, _U64, _VP, _VP]),
+    "gpda_expected_hist_adjoint": (_I32, [_VP, _I32, _I32, _VP, _VP, _I32, _U64, _VP, _VP, _VP]),
+    "gpda_expected_grad": (_I32, [_VP, _I32, _I32, _VP, _VP, _I32, _U64, _VP, _VP, _VP, _VP]),
     "gpda_run_pda_noalloc": (_I32, [C.POINTER(GpdaModel), _I32, _I32, _I32, _VP, _VP, _VP, _VP, _VP,
                                     _I64, _I32, _U64, _VP, _VP, _VP, _VP]),
     "gpda_mc_create": (_VP, [_I32, _I32, C.c_uint8, _U64, _I32, _P_I32]),

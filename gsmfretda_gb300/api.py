@@ -120,6 +120,46 @@ class Engine:
                                        _p(units), _p(hist)), self.ctx)
         return units, hist
 
+    # ---------------------------------------------------------------- expected histogram
+    def _exp_args(self, n, args, anchor):
+        a = np.ascontiguousarray(args, dtype=np.float32).reshape(-1)
+        P = a.size // (n * (n + 1))
+        an = None if anchor is None else np.ascontiguousarray(anchor, dtype=np.float32).reshape(-1)
+        if an is not None and an.size != a.size:
+            raise ValueError("anchor must have the shape of args")
+        return a, an, P
+
+    def expected_hist(self, n, args, samples, seed, anchor=None):
+        """Differentiable expected-histogram form (occupancy model, V = 0):
+        expected counts (P, nbins) summed over samples and chi2 (P,)."""
+        a, an, P = self._exp_args(n, args, anchor)
+        hist = np.zeros((P, self.nbins), dtype=np.float64)
+        chi2 = np.zeros(P, dtype=np.float64)
+        _check(self.lib.gpda_expected_hist(self.ctx, P, n, _p(a), _p(an), samples, seed,
+                                           _p(hist), _p(chi2)), self.ctx)
+        return hist, chi2
+
+    def expected_adjoint(self, n, args, samples, seed, anchor=None, dchi2=None):
+        """Gradient of sum(dchi2 * chi2) in E (P, n) and ln K (P, n(n-1))."""
+        a, an, P = self._exp_args(n, args, anchor)
+        up = None if dchi2 is None else np.ascontiguousarray(dchi2, dtype=np.float64).reshape(P)
+        dE = np.zeros((P, n), dtype=np.float64)
+        dK = np.zeros((P, n * (n - 1)), dtype=np.float64)
+        _check(self.lib.gpda_expected_hist_adjoint(self.ctx, P, n, _p(a), _p(an), samples, seed,
+                                                   _p(up), _p(dE), _p(dK)), self.ctx)
+        return dE, dK
+
+    def expected_grad(self, n, args, samples, seed, anchor=None):
+        """Forward and gradient in one call: hist, chi2, dE, dlnK."""
+        a, an, P = self._exp_args(n, args, anchor)
+        hist = np.zeros((P, self.nbins), dtype=np.float64)
+        chi2 = np.zeros(P, dtype=np.float64)
+        dE = np.zeros((P, n), dtype=np.float64)
+        dK = np.zeros((P, n * (n - 1)), dtype=np.float64)
+        _check(self.lib.gpda_expected_grad(self.ctx, P, n, _p(a), _p(an), samples, seed, _p(hist),
+                                           _p(chi2), _p(dE), _p(dK)), self.ctx)
+        return hist, chi2, dE, dK
+
     def launch(self, mode, n, args, samples, seed, b0=0, b1=None):
         """Asynchronous: returns after the launch is queued on the context stream."""
         b1 = self.B if b1 is None else b1

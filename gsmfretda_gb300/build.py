@@ -18,7 +18,8 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libgpda.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
-SOURCES = ["gpda_kernels.cu", "gpda_engine.cu", "gpda_mc.cu", "gpda_params.cpp", "gpda_noalloc.cu"]
+SOURCES = ["gpda_kernels.cu", "gpda_engine.cu", "gpda_mc.cu", "gpda_params.cpp", "gpda_noalloc.cu",
+           "gpda_expected.cu"]
 HEADERS = ["gpda_device.cuh", "gpda_internal.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-prec-div=true", "-prec-sqrt=true",

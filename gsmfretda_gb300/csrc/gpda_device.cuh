@@ -46,7 +46,7 @@ __device__ __forceinline__ uint4 philox_block_inline(uint32_t x0, uint32_t x1, u
 // The same block behind one out-of-line copy: the draw sites of the samplers
 // call it instead of carrying their own inlined rounds, which keeps the
 // instruction footprint of the simulation loop small.
-__device__ __noinline__ uint4 philox_block(uint32_t x0, uint32_t x1, uint32_t x2, uint32_t x3,
+static __device__ __noinline__ uint4 philox_block(uint32_t x0, uint32_t x1, uint32_t x2, uint32_t x3,
                                            uint32_t a, uint32_t b) {
     return philox_block_inline(x0, x1, x2, x3, a, b);
 }
@@ -78,6 +78,9 @@ struct Rng {
     // discarded): keeps block generation at the same program point for all
     // lanes of a warp.
     __device__ __forceinline__ void align() { idx = 4; }
+    // The next draw starts at counter block `b` (a stream position that does
+    // not depend on how many draws came before).
+    __device__ __forceinline__ void seek(uint32_t b) { blk = b; idx = 4; }
     // align() + generate that block now, inline; only where at least one
     // draw follows before the next align (same words as align()).
     __device__ __forceinline__ void align_now() {
@@ -408,6 +411,42 @@ __device__ __forceinline__ float eps_of(float e, float g, float ct) {
     float om = 1.0f - e;
     float num = g * e + ct * om;
     return num / (num + om);
+}
+
+// ---------------------------------------------------------------- model draws
+// Categorical draw over a cumulative table; jump to a state other than `from`.
+__device__ __forceinline__ int cat_draw(const float *cdf, int n, float u) {
+    for (int i = 0; i < n; ++i)
+        if (u <= cdf[i]) return i;
+    return n - 1;
+}
+
+__device__ __forceinline__ int jump_draw(const float *row, int n, int from, float u) {
+    int last = from;
+    for (int i = 0; i < n; ++i) {
+        if (i == from) continue;
+        last = i;
+        if (u <= row[i]) return i;
+    }
+    return last;
+}
+
+// Background of one window (Poisson, clipped as draw_P_B_Tr does,
+// src/gen_rand.cuh:92-107), acceptor channel first; returns the acceptor
+// background, writes the remaining signal photons to *sig.
+__device__ __forceinline__ int background(Rng &r, int navail, float lam_a, float lam_d, int *sig,
+                                          int &lim, const float *inv) {
+    int B[2];
+    int avail = navail;
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+        int x = poisson(r, c == 0 ? lam_a : lam_d, lim, inv);
+        if (x > avail) x = (int)floorf((float)avail * r.u01());
+        B[c] = x;
+        avail -= x;
+    }
+    *sig = avail;
+    return B[0];
 }
 
 }  // namespace gpda

@@ -62,6 +62,20 @@ struct gpda_ctx {
     float *dCdf = nullptr;          // photon-mode binomial tables
     uint16_t *dGuide = nullptr;
     size_t cap_tab = 0;             // in (parameter set, state) tables
+    // expected-histogram path
+    ExpParams *dExp = nullptr;
+    ExpParams *hExp = nullptr;      // pinned
+    int cap_exp_P = 0;
+    double *dExpPart = nullptr, *dExpGPart = nullptr;
+    size_t cap_exp_part = 0;        // in P * nblk
+    double *dExpHist = nullptr, *dExpChi2 = nullptr, *dExpGrad = nullptr, *dExpUp = nullptr;
+    float *dExpG = nullptr;
+    double *hExpOut = nullptr;      // pinned: chi2[P], hist[P][nbins], grad[P][16], up[P]
+    int cap_exp_out = 0;            // in P
+    float *dExpInv = nullptr;
+    bool exp_valid = false;         // the forward state matches exp_key
+    std::vector<float> exp_key;
+    int exp_P = 0, exp_nblk = 0;
     // last launch
     int last_P = 0;
     bool last_chi2 = false;
@@ -229,6 +243,162 @@ int do_launch(gpda_ctx *c, int mode, int P, int n, const float *params, int64_t 
     return GPDA_OK;
 }
 
+// ---------------------------------------------------------------- expected histogram
+
+int exp_prepare(gpda_ctx *c, int P, int n, const float *params, const float *anchor, int S,
+                uint64_t seed, ExpArgs &a) {
+    if (P < 1 || n < 1 || S < 1 || !params) return fail(c, GPDA_ERR_ARG, "P, n_states, samples or params");
+    if (n > kExpMaxStates) return fail(c, GPDA_ERR_LIMIT, "expected histogram: at most 4 states");
+    if (c->model.nbins > kExpMaxBins) return fail(c, GPDA_ERR_LIMIT, "expected histogram: at most 64 bins");
+    if (c->B == 0 || !c->dN) return fail(c, GPDA_ERR_STATE, "no bursts uploaded");
+    if (!c->has_obs) return fail(c, GPDA_ERR_STATE, "no observed histogram");
+    if (c->B * (int64_t)S > (int64_t)1 << 40) return fail(c, GPDA_ERR_ARG, "too many units");
+    CK(cudaSetDevice(c->device));
+    CK(cudaStreamSynchronize(c->stream));   // pinned staging and scratch are free
+    const int nb = c->model.nbins;
+    const int nblk = exp_blocks_per_param(P, c->B * (int64_t)S, c->num_sms);
+    if (!c->dExpInv) {
+        CK(cudaMalloc(&c->dExpInv, sizeof(float) * kExpInvN));
+        CK(launch_exp_inv_table(c->dExpInv, c->stream));
+        c->launches += 1;
+    }
+    if (P > c->cap_exp_out) {
+        free_dev(c->dExp); free_dev(c->dExpHist); free_dev(c->dExpChi2); free_dev(c->dExpGrad);
+        free_dev(c->dExpUp); free_dev(c->dExpG);
+        if (c->hExp) cudaFreeHost(c->hExp);
+        if (c->hExpOut) cudaFreeHost(c->hExpOut);
+        c->dExp = nullptr; c->dExpHist = nullptr; c->dExpChi2 = nullptr; c->dExpGrad = nullptr;
+        c->dExpUp = nullptr; c->dExpG = nullptr; c->hExp = nullptr; c->hExpOut = nullptr;
+        c->cap_exp_out = 0;
+        CK(cudaMalloc(&c->dExp, sizeof(ExpParams) * P));
+        CK(cudaMallocHost(&c->hExp, sizeof(ExpParams) * P));
+        CK(cudaMalloc(&c->dExpHist, sizeof(double) * (size_t)P * kExpMaxBins));
+        CK(cudaMalloc(&c->dExpChi2, sizeof(double) * P));
+        CK(cudaMalloc(&c->dExpGrad, sizeof(double) * (size_t)P * kExpGrad));
+        CK(cudaMalloc(&c->dExpUp, sizeof(double) * P));
+        CK(cudaMalloc(&c->dExpG, sizeof(float) * (size_t)P * kExpMaxBins));
+        CK(cudaMallocHost(&c->hExpOut, sizeof(double) * (size_t)P * (2 + kExpMaxBins + kExpGrad)));
+        c->cap_exp_out = P;
+    }
+    const size_t parts = (size_t)P * nblk;
+    if (parts > c->cap_exp_part) {
+        free_dev(c->dExpPart); free_dev(c->dExpGPart);
+        c->dExpPart = nullptr; c->dExpGPart = nullptr; c->cap_exp_part = 0;
+        CK(cudaMalloc(&c->dExpPart, sizeof(double) * parts * kExpMaxBins));
+        CK(cudaMalloc(&c->dExpGPart, sizeof(double) * parts * kExpGrad));
+        c->cap_exp_part = parts;
+    }
+    const size_t stride = (size_t)n * (n + 1);
+    for (int p = 0; p < P; ++p) {
+        const float *th = params + stride * p;
+        const float *an = anchor ? anchor + stride * p : th;
+        int r = build_exp_params(n, th, an, c->model.gamma, c->model.crosstalk, &c->hExp[p]);
+        if (r == -2) return fail(c, GPDA_ERR_SINGULAR, "rate matrix has no unique stationary distribution (parameter set " + std::to_string(p) + ")");
+        if (r != 0) return fail(c, GPDA_ERR_ARG, "invalid parameter vector " + std::to_string(p) + " (the expected form needs V = 0)");
+    }
+    CK(cudaMemcpyAsync(c->dExp, c->hExp, sizeof(ExpParams) * P, cudaMemcpyHostToDevice, c->stream));
+    a = ExpArgs{};
+    a.N = c->dN;
+    a.T = c->dT;
+    a.params = c->dExp;
+    a.obs = c->dObs;
+    a.inv = c->dExpInv;
+    a.part = c->dExpPart;
+    a.hist = c->dExpHist;
+    a.chi2 = c->dExpChi2;
+    a.g = c->dExpG;
+    a.gpart = c->dExpGPart;
+    a.grad = c->dExpGrad;
+    a.dchi2 = nullptr;
+    a.limit_hits = c->dLimit;
+    a.B = c->B;
+    a.S = S;
+    a.P = P;
+    a.nbins = nb;
+    a.left_pad = c->model.left_pad;
+    a.nblk = nblk;
+    a.n = n;
+    a.seed = seed;
+    a.gamma = c->model.gamma;
+    a.ct = c->model.crosstalk;
+    a.bg_a = c->model.bg_a;
+    a.bg_d = c->model.bg_d;
+    return GPDA_OK;
+}
+
+std::vector<float> exp_make_key(int P, int n, const float *params, const float *anchor, int S,
+                                uint64_t seed) {
+    const size_t m = (size_t)P * n * (n + 1);
+    std::vector<float> k;
+    k.reserve(2 * m + 6);
+    k.push_back((float)P);
+    k.push_back((float)n);
+    k.push_back((float)S);
+    float sw[2];
+    std::memcpy(sw, &seed, 8);
+    k.push_back(sw[0]);
+    k.push_back(sw[1]);
+    k.insert(k.end(), params, params + m);
+    k.push_back(anchor ? 1.0f : 0.0f);
+    if (anchor) k.insert(k.end(), anchor, anchor + m);
+    return k;
+}
+
+bool exp_same_key(const std::vector<float> &a, const std::vector<float> &b) {
+    return a.size() == b.size() && std::memcmp(a.data(), b.data(), sizeof(float) * a.size()) == 0;
+}
+
+// forward + (optionally) adjoint; outputs copied once at the end
+int exp_run(gpda_ctx *c, int P, int n, const float *params, const float *anchor, int S,
+            uint64_t seed, double *hist_out, double *chi2_out, bool adjoint, const double *dchi2,
+            double *dE, double *dlogK) {
+    auto key = exp_make_key(P, n, params, anchor, S, seed);
+    ExpArgs a;
+    bool need_fwd = !(adjoint && c->exp_valid && exp_same_key(key, c->exp_key)) || hist_out || chi2_out;
+    int rc = exp_prepare(c, P, n, params, anchor, S, seed, a);
+    if (rc) { c->exp_valid = false; return rc; }
+    const int nb = c->model.nbins;
+    double *hc = c->hExpOut;                                 // chi2[P]
+    double *hh = hc + P;                                     // hist[P][nbins]
+    double *hg = hh + (size_t)P * kExpMaxBins;               // grad[P][16]
+    double *hu = hg + (size_t)P * kExpGrad;                  // up[P]
+    CK(cudaEventRecord(c->k0, c->stream));
+    if (need_fwd) {
+        c->exp_valid = false;
+        CK(launch_exp_forward(a, c->stream));
+        c->launches += 2;
+        c->exp_key = key;
+        c->exp_P = P;
+        c->exp_nblk = a.nblk;
+    }
+    if (adjoint) {
+        if (dchi2) {
+            std::memcpy(hu, dchi2, sizeof(double) * P);
+            CK(cudaMemcpyAsync(c->dExpUp, hu, sizeof(double) * P, cudaMemcpyHostToDevice, c->stream));
+            a.dchi2 = c->dExpUp;
+        }
+        CK(launch_exp_adjoint(a, c->stream));
+        c->launches += 2;
+    }
+    CK(cudaEventRecord(c->k1, c->stream));
+    c->timed = true;
+    if (chi2_out) CK(cudaMemcpyAsync(hc, c->dExpChi2, sizeof(double) * P, cudaMemcpyDeviceToHost, c->stream));
+    if (hist_out) CK(cudaMemcpyAsync(hh, c->dExpHist, sizeof(double) * (size_t)P * nb, cudaMemcpyDeviceToHost, c->stream));
+    if (adjoint) CK(cudaMemcpyAsync(hg, c->dExpGrad, sizeof(double) * (size_t)P * kExpGrad, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    c->exp_valid = true;
+    if (chi2_out) std::memcpy(chi2_out, hc, sizeof(double) * P);
+    if (hist_out) std::memcpy(hist_out, hh, sizeof(double) * (size_t)P * nb);
+    if (adjoint) {
+        const int nk = n * (n - 1);
+        for (int p = 0; p < P; ++p) {
+            if (dE) for (int i = 0; i < n; ++i) dE[(size_t)p * n + i] = hg[(size_t)p * kExpGrad + i];
+            if (dlogK) for (int k = 0; k < nk; ++k) dlogK[(size_t)p * nk + k] = hg[(size_t)p * kExpGrad + n + k];
+        }
+    }
+    return GPDA_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -297,6 +467,11 @@ void gpda_destroy(gpda_ctx *c) {
     free_dev(c->dObs); free_dev(c->dParams); free_dev(c->dHist); free_dev(c->dChi2);
     free_dev(c->dWork); free_dev(c->dLimit); free_dev(c->dUnit); free_dev(c->dFlag);
     free_dev(c->dCdf); free_dev(c->dGuide);
+    free_dev(c->dExp); free_dev(c->dExpPart); free_dev(c->dExpGPart); free_dev(c->dExpHist);
+    free_dev(c->dExpChi2); free_dev(c->dExpGrad); free_dev(c->dExpUp); free_dev(c->dExpG);
+    free_dev(c->dExpInv);
+    if (c->hExp) cudaFreeHost(c->hExp);
+    if (c->hExpOut) cudaFreeHost(c->hExpOut);
     if (c->hFlag) cudaFreeHost(c->hFlag);
     if (c->k0) cudaEventDestroy(c->k0);
     if (c->k1) cudaEventDestroy(c->k1);
@@ -323,6 +498,7 @@ int32_t gpda_upload_bursts(gpda_ctx *c, const int32_t *N, const float *T, const 
     CK(cudaSetDevice(c->device));
     CK(cudaStreamSynchronize(c->stream));
     c->B = 0;
+    c->exp_valid = false;
     // grow-only device store; contents are validated on the device below
     if (B > c->cap_B) {
         free_dev(c->dN); free_dev(c->dT); free_dev(c->dOffIdx);
@@ -372,6 +548,7 @@ int32_t gpda_upload_bursts(gpda_ctx *c, const int32_t *N, const float *T, const 
 }
 
 int32_t gpda_set_observed(gpda_ctx *c, const float *ohist, int32_t nbins) {
+    if (c) c->exp_valid = false;
     if (!c) return GPDA_ERR_ARG;
     if (!ohist || nbins != c->model.nbins) return fail(c, GPDA_ERR_ARG, "observed histogram must have model.nbins bins");
     CK(cudaSetDevice(c->device));
@@ -500,6 +677,30 @@ int64_t gpda_limit_hits(gpda_ctx *c) {
     if (cudaMemcpyAsync(&v, c->dLimit, sizeof(v), cudaMemcpyDeviceToHost, c->stream) != cudaSuccess) return GPDA_ERR_CUDA;
     if (cudaStreamSynchronize(c->stream) != cudaSuccess) return GPDA_ERR_CUDA;
     return (int64_t)v;
+}
+
+int32_t gpda_expected_hist(gpda_ctx *c, int32_t P, int32_t n, const float *params,
+                           const float *anchor, int32_t S, uint64_t seed, double *hist_out,
+                           double *chi2_out) {
+    if (!c) return GPDA_ERR_ARG;
+    if (!chi2_out) return fail(c, GPDA_ERR_ARG, "chi2_out");
+    return exp_run(c, P, n, params, anchor, S, seed, hist_out, chi2_out, false, nullptr, nullptr, nullptr);
+}
+
+int32_t gpda_expected_hist_adjoint(gpda_ctx *c, int32_t P, int32_t n, const float *params,
+                                   const float *anchor, int32_t S, uint64_t seed,
+                                   const double *dchi2, double *dE, double *dlogK) {
+    if (!c) return GPDA_ERR_ARG;
+    if (!dE && !dlogK) return fail(c, GPDA_ERR_ARG, "dE or dlogK");
+    return exp_run(c, P, n, params, anchor, S, seed, nullptr, nullptr, true, dchi2, dE, dlogK);
+}
+
+int32_t gpda_expected_grad(gpda_ctx *c, int32_t P, int32_t n, const float *params,
+                           const float *anchor, int32_t S, uint64_t seed, double *hist_out,
+                           double *chi2_out, double *dE, double *dlogK) {
+    if (!c) return GPDA_ERR_ARG;
+    if (!chi2_out) return fail(c, GPDA_ERR_ARG, "chi2_out");
+    return exp_run(c, P, n, params, anchor, S, seed, hist_out, chi2_out, true, nullptr, dE, dlogK);
 }
 
 }  // extern "C"

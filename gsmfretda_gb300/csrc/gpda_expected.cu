@@ -1,0 +1,501 @@
+// gpda_expected.cu — differentiable expected-histogram PDA (occupancy model)
+// and its adjoint, sm_103a.
+//
+// Per unit (parameter set p, burst b, dwell sample s) the state skeleton is
+// the sampled occupancy model's, drawn from the same Philox counters
+// (seed, pword = p, b, s) in the same order (step_occ in gpda_kernels.cu); it
+// comes from the anchor theta0 and carries the likelihood-ratio weight W (see
+// ExpParams). The background counts are drawn as in step_occ but from counter
+// block 2^31 on, so that they do not depend on the trajectory's length. With
+//   E_eff = sum_k dt_k E[s_k] / T,  dt_k = -ln(u_k) / k_exit(s_k; theta)
+//   p     = eps(E_eff) = (g E + ct (1-E)) / (g E + (1+ct)(1-E))
+// the unit adds W * P(X = x), X ~ Binomial(sig, p), to the bin of the
+// proximity ratio (ba + x) / N for every x; sig and ba are the signal photons
+// and acceptor background left by the background draw.
+//
+// Binomial masses: the mode's probability by Loader's saddle-point form
+// (C. Loader, "Fast and accurate computation of binomial probabilities",
+// 2000), then the ratio recurrence P(x+1)/P(x) = (sig-x) p / ((x+1) q) in both
+// directions until a mass drops below 2^-30 of the mode's.
+//
+// Kernels (one parameter set per blockIdx.y, units strided over blockIdx.x):
+//   exp_fwd_kernel   per-thread FP32 bin rows in shared memory, reduced in a
+//                    fixed order into per-block FP64 partials
+//   exp_chi2_kernel  partials -> expected counts, reduced chi-square (FP64,
+//                    sequential over bins as chi2_kernel) and d chi2 / d count
+//   exp_adj_kernel   re-walks each unit: G = sum g_bin P(x), H = d G / d p,
+//                    and the pathwise (dwells, E) plus score (skeleton) terms
+//   exp_grad_kernel  per-block partials -> gradient, times the upstream d chi2
+// All sums have a fixed order, so results do not depend on scheduling.
+#include <algorithm>
+
+#include "gpda_device.cuh"
+#include "gpda_internal.h"
+
+namespace gpda {
+
+namespace {
+
+constexpr int kExpThreads = 256;
+constexpr float kMassCut = 0x1p-30f;
+constexpr uint32_t kExpBgBlock = 0x80000000u;   // above any trajectory block (< 2^15)
+
+// ln(1 - x) for 0 <= x < 1 without forming 1 - x when x is small
+__device__ __forceinline__ float log1m_(float x) {
+    if (x < 0.01f) {
+        float x2 = x * x;
+        return -(x + x2 * (0.5f + x * (0.333333343f + x * (0.25f + x * 0.2f))));
+    }
+    return logf_(1.0f - x);
+}
+
+// Loader's deviance term bd0(x, np) = x ln(x / np) + np - x, by its series
+// when x is close to np.
+__device__ __forceinline__ float bd0(float x, float np) {
+    float d = x - np;
+    if (fabsf(d) < 0.1f * (x + np)) {
+        float v = d / (x + np);
+        float s = d * v;
+        float ej = 2.0f * x * v;
+        float v2 = v * v;
+        for (int j = 1; j < 16; ++j) {
+            ej = ej * v2;
+            float s1 = s + ej / (float)(2 * j + 1);
+            if (s1 == s) return s1;
+            s = s1;
+        }
+        return s;
+    }
+    return x * logf_(x / np) + np - x;
+}
+
+// stirlerr(k) = ln k! - (k + 1/2) ln k + k - ln(2 pi)/2 = fc(k - 1), k >= 1
+__device__ __forceinline__ float stirlerr(int k) { return fc((float)(k - 1)); }
+
+// P(X = m) for X ~ Binomial(n, p), 0 < p < 1, q = 1 - p
+__device__ __forceinline__ float binom_pmf(int n, int m, float p, float q) {
+    if (m == 0) return expf_((float)n * log1m_(p));
+    if (m == n) return expf_((float)n * log1m_(q));
+    float fn = (float)n;
+    float lc = stirlerr(n) - stirlerr(m) - stirlerr(n - m) - bd0((float)m, fn * p) -
+               bd0((float)(n - m), fn * q);
+    const float inv2pi = 0.159154943091895336f;
+    return expf_(lc) * sqrtf(fn * inv2pi / ((float)m * (float)(n - m)));
+}
+
+__device__ __forceinline__ float inv_of(const float *inv, int k) {
+    return (k < kExpInvN) ? __ldg(inv + k) : 1.0f / (float)k;
+}
+
+// first acceptor count a with floor(a * nbins / N) >= b
+__device__ __forceinline__ int bin_start(int b, int N, int nbins) {
+    return (int)(((int64_t)b * N + nbins - 1) / nbins);
+}
+
+__device__ __forceinline__ int bin_of(int a, int N, int nbins) {
+    int b = (int)(((int64_t)a * nbins) / N);
+    return b < nbins - 1 ? b : nbins - 1;
+}
+
+template <int NS>
+struct ExpUnit {
+    float acc;          // sum dt E
+    float lw;           // log weight
+    float dtl;          // duration of the last segment
+    int s0, sm;         // first and last state
+    float D[NS];        // time in each state over the segments before the last
+    int cnt[NS][NS];    // jumps from -> to
+};
+
+// The trajectory of one unit under (skeleton theta0, dwells theta), then the
+// background; returns false when the burst has no photons.
+template <int NS, bool STATS>
+__device__ __forceinline__ bool exp_walk(const ExpParams &P, Rng &r, int Nb, float Tb, float bga,
+                                         float bgd, ExpUnit<NS> &U, int &sig, int &ba, int &lim,
+                                         const float *sinv) {
+    U.acc = 0.0f;
+    U.lw = 0.0f;
+    U.dtl = 0.0f;
+    if (STATS) {
+#pragma unroll
+        for (int i = 0; i < NS; ++i) {
+            U.D[i] = 0.0f;
+#pragma unroll
+            for (int j = 0; j < NS; ++j) U.cnt[i][j] = 0;
+        }
+    }
+    float t = 0.0f;
+    int st = 0;
+    for (int seg = 0; seg < kMaxSeg; ++seg) {
+        const float us = r.u01();
+        int ns;
+        if (seg == 0) {
+            ns = cat_draw(P.init_cdf, NS, us);
+            U.s0 = ns;
+            U.lw += P.lw_init[ns];
+        } else {
+            ns = jump_draw(P.jump_cdf + st * 4, NS, st, us);
+            U.lw += P.lw_jump[st * 4 + ns];
+            if (STATS) {
+#pragma unroll
+                for (int i = 0; i < NS; ++i)
+#pragma unroll
+                    for (int j = 0; j < NS; ++j)
+                        if (i == st && j == ns) U.cnt[i][j] += 1;
+            }
+        }
+        st = ns;
+        if (!(Tb > 0.0f)) break;
+        float u = r.u01();
+        float tau = (P.kexit[st] > 0.0f) ? (-logf_(u)) * P.inv_kexit[st] : kInf;
+        float tn = t + tau;
+        bool cut = seg == kMaxSeg - 1;
+        bool last = !(tn < Tb) || cut;
+        if (cut && tn < Tb) lim += 1;
+        float dt = last ? Tb - t : tn - t;
+        U.acc = fmaf(dt, P.E[st], U.acc);
+        if (last) {
+            U.dtl = dt;
+            break;
+        }
+        if (STATS) {
+#pragma unroll
+            for (int i = 0; i < NS; ++i)
+                if (i == st) U.D[i] += dt;
+        }
+        t = tn;
+    }
+    U.sm = st;
+    // the background comes from a fixed block, so that its counts do not
+    // change when a dwell crosses the end of the burst
+    r.seek(kExpBgBlock);
+    ba = background(r, Nb, bga * Tb, bgd * Tb, &sig, lim, sinv);
+    return Nb > 0;
+}
+
+__device__ __forceinline__ float eps_p(float e, float g, float ct) { return eps_of(e, g, ct); }
+
+// d eps / d E
+__device__ __forceinline__ float eps_dp(float e, float g, float ct) {
+    float om = 1.0f - e;
+    float num = g * e + ct * om;
+    float den = num + om;
+    return ((g - ct) * om + num) / (den * den);
+}
+
+// Walks the masses of (ba + X) / N, X ~ Binomial(sig, p), one bin run at a
+// time: F(bin, run mass, run sum of x * mass) is called once per bin touched.
+template <class F>
+__device__ __forceinline__ void binom_bins(int Nb, int sig, int ba, float p, int nbins,
+                                           const float *inv, F &&flush) {
+    if (sig <= 0 || !(p > 0.0f)) {
+        flush(bin_of(ba, Nb, nbins), 1.0f, 0.0f);
+        return;
+    }
+    if (p >= 1.0f) {
+        flush(bin_of(ba + sig, Nb, nbins), 1.0f, (float)sig);
+        return;
+    }
+    const float q = 1.0f - p;
+    int m = (int)((float)(sig + 1) * p);
+    if (m > sig) m = sig;
+    const float w0 = binom_pmf(sig, m, p, q);
+    const float cut = w0 * kMassCut;
+    const float rho = p / q, irho = q / p;
+    // upward from the mode
+    {
+        int b = bin_of(ba + m, Nb, nbins);
+        int a_next = (b < nbins - 1) ? bin_start(b + 1, Nb, nbins) : 0x7fffffff;
+        float w = w0, run = 0.0f, runx = 0.0f;
+        for (int x = m; x <= sig; ++x) {
+            if (ba + x >= a_next) {
+                flush(b, run, runx);
+                run = 0.0f;
+                runx = 0.0f;
+                b = bin_of(ba + x, Nb, nbins);
+                a_next = (b < nbins - 1) ? bin_start(b + 1, Nb, nbins) : 0x7fffffff;
+            }
+            run += w;
+            runx = fmaf((float)x, w, runx);
+            if (x == sig) break;
+            w = w * ((float)(sig - x) * rho) * inv_of(inv, x + 1);
+            if (w < cut) break;
+        }
+        flush(b, run, runx);
+    }
+    // downward from the mode
+    if (m > 0) {
+        float w = w0 * ((float)m * irho) * inv_of(inv, sig - m + 1);
+        if (w >= cut) {
+            int b = bin_of(ba + m - 1, Nb, nbins);
+            int a_lo = bin_start(b, Nb, nbins);
+            float run = 0.0f, runx = 0.0f;
+            for (int x = m - 1; x >= 0; --x) {
+                if (ba + x < a_lo) {
+                    flush(b, run, runx);
+                    run = 0.0f;
+                    runx = 0.0f;
+                    b = bin_of(ba + x, Nb, nbins);
+                    a_lo = bin_start(b, Nb, nbins);
+                }
+                run += w;
+                runx = fmaf((float)x, w, runx);
+                if (x == 0) break;
+                w = w * ((float)x * irho) * inv_of(inv, sig - x + 1);
+                if (w < cut) break;
+            }
+            flush(b, run, runx);
+        }
+    }
+}
+
+// sum of v[t * stride] over the block's threads in a fixed order, FP64;
+// warp w of the block reduces the values it is given
+__device__ __forceinline__ double warp_sum_fixed(const float *col, int lane) {
+    double v = 0.0;
+    for (int t = lane; t < kExpThreads; t += 32) v += (double)col[t];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+template <int NS>
+__global__ void __launch_bounds__(kExpThreads) exp_fwd_kernel(const ExpArgs a) {
+    extern __shared__ float sh_rows[];          // [nbins][kExpThreads]
+    __shared__ float s_inv[kInvTable];
+    __shared__ ExpParams sP;
+    const int tid = threadIdx.x;
+    const int p = blockIdx.y;
+    if (tid < kInvTable) s_inv[tid] = tid > 0 ? 1.0f / (float)tid : 0.0f;
+    if (tid < 128) reinterpret_cast<float *>(&sP)[tid] = reinterpret_cast<const float *>(a.params + p)[tid];
+    for (int i = tid; i < a.nbins * kExpThreads; i += kExpThreads) sh_rows[i] = 0.0f;
+    __syncthreads();
+    const int64_t units = a.B * (int64_t)a.S;
+    const int64_t stride = (int64_t)a.nblk * kExpThreads;
+    int lim = 0;
+    float *row = sh_rows + tid;
+    for (int64_t u = (int64_t)blockIdx.x * kExpThreads + tid; u < units; u += stride) {
+        const int b = (int)(u / a.S);
+        const int s = (int)(u - (int64_t)b * a.S);
+        const int Nb = __ldg(a.N + b);
+        const float Tb = __ldg(a.T + b);
+        Rng r;
+        r.init(a.seed, (uint32_t)p, (uint32_t)b, (uint32_t)s);
+        ExpUnit<NS> U;
+        int sig, ba;
+        if (!exp_walk<NS, false>(sP, r, Nb, Tb, a.bg_a, a.bg_d, U, sig, ba, lim, s_inv)) continue;
+        const float eeff = (Tb > 0.0f) ? U.acc / Tb : sP.E[U.sm];
+        const float W = expf_(U.lw);
+        const float pe = eps_p(eeff, a.gamma, a.ct);
+        binom_bins(Nb, sig, ba, pe, a.nbins, a.inv, [&](int bin, float m, float) {
+            row[bin * kExpThreads] += W * m;
+        });
+    }
+    if (lim) atomicAdd(a.limit_hits, (unsigned long long)lim);
+    __syncthreads();
+    const int warp = tid >> 5, lane = tid & 31;
+    double *out = a.part + ((size_t)p * a.nblk + blockIdx.x) * a.nbins;
+    for (int bin = warp; bin < a.nbins; bin += kExpThreads / 32) {
+        double v = warp_sum_fixed(sh_rows + bin * kExpThreads, lane);
+        if (lane == 0) out[bin] = v;
+    }
+}
+
+// One block per parameter set, one thread per bin.
+__global__ void exp_chi2_kernel(const ExpArgs a) {
+    __shared__ double sM[kExpMaxBins];
+    const int p = blockIdx.x;
+    const int bin = threadIdx.x;
+    if (bin < a.nbins) {
+        const double *src = a.part + (size_t)p * a.nblk * a.nbins + bin;
+        double v = 0.0;
+        for (int k = 0; k < a.nblk; ++k) v += src[(size_t)k * a.nbins];
+        sM[bin] = v;
+        a.hist[(size_t)p * a.nbins + bin] = v;
+    }
+    __syncthreads();
+    if (bin != 0) return;
+    int effN = a.nbins - a.left_pad;
+    double chi = 0.0;
+    for (int i = a.left_pad; i < a.nbins; ++i) {
+        if (sM[i] > 0.0) {
+            double mi = sM[i] / (double)a.S;
+            double d = (double)a.obs[i] - mi;
+            chi = chi + d * d / mi;
+        } else {
+            effN -= 1;
+        }
+    }
+    const double den = (double)(effN - a.n * (a.n + 1));
+    a.chi2[p] = chi / den;
+    float *g = a.g + (size_t)p * a.nbins;
+    for (int i = 0; i < a.nbins; ++i) {
+        double gi = 0.0;
+        if (i >= a.left_pad && sM[i] > 0.0) {
+            double mi = sM[i] / (double)a.S;
+            double o = (double)a.obs[i];
+            gi = (1.0 - (o * o) / (mi * mi)) / ((double)a.S * den);
+        }
+        g[i] = (float)gi;
+    }
+}
+
+template <int NS>
+__global__ void __launch_bounds__(kExpThreads) exp_adj_kernel(const ExpArgs a) {
+    constexpr int NG = NS + NS * (NS - 1);
+    __shared__ float s_inv[kInvTable];
+    __shared__ float s_g[kExpMaxBins];
+    __shared__ float s_red[NG][kExpThreads];
+    __shared__ ExpParams sP;
+    const int tid = threadIdx.x;
+    const int p = blockIdx.y;
+    if (tid < kInvTable) s_inv[tid] = tid > 0 ? 1.0f / (float)tid : 0.0f;
+    if (tid < 128) reinterpret_cast<float *>(&sP)[tid] = reinterpret_cast<const float *>(a.params + p)[tid];
+    if (tid < a.nbins) s_g[tid] = a.g[(size_t)p * a.nbins + tid];
+    __syncthreads();
+    float gacc[NG];
+#pragma unroll
+    for (int k = 0; k < NG; ++k) gacc[k] = 0.0f;
+    const int64_t units = a.B * (int64_t)a.S;
+    const int64_t stride = (int64_t)a.nblk * kExpThreads;
+    int lim = 0;
+    for (int64_t u = (int64_t)blockIdx.x * kExpThreads + tid; u < units; u += stride) {
+        const int b = (int)(u / a.S);
+        const int s = (int)(u - (int64_t)b * a.S);
+        const int Nb = __ldg(a.N + b);
+        const float Tb = __ldg(a.T + b);
+        Rng r;
+        r.init(a.seed, (uint32_t)p, (uint32_t)b, (uint32_t)s);
+        ExpUnit<NS> U;
+        int sig, ba;
+        if (!exp_walk<NS, true>(sP, r, Nb, Tb, a.bg_a, a.bg_d, U, sig, ba, lim, s_inv)) continue;
+        const bool timed = Tb > 0.0f;
+        const float eeff = timed ? U.acc / Tb : sP.E[U.sm];
+        const float W = expf_(U.lw);
+        const float pe = eps_p(eeff, a.gamma, a.ct);
+        float G = 0.0f, GX = 0.0f;
+        binom_bins(Nb, sig, ba, pe, a.nbins, a.inv, [&](int bin, float m, float mx) {
+            const float gb = s_g[bin];
+            G = fmaf(gb, m, G);
+            GX = fmaf(gb, mx, GX);
+        });
+        // H = sum g P'(x) = (sum g x P - sig p sum g P) / (p q); zero at p in {0, 1}
+        float H = 0.0f;
+        if (sig > 0 && pe > 0.0f && pe < 1.0f) H = (GX - (float)sig * pe * G) / (pe * (1.0f - pe));
+        const float HE = W * H * eps_dp(eeff, a.gamma, a.ct);
+        const float WG = W * G;
+        // d / d E_s: occupancy fraction of state s
+        const float invT = timed ? 1.0f / Tb : 0.0f;
+#pragma unroll
+        for (int i = 0; i < NS; ++i) {
+            float occ;
+            if (timed) occ = (U.D[i] + (i == U.sm ? U.dtl : 0.0f)) * invT;
+            else occ = (i == U.sm) ? 1.0f : 0.0f;
+            gacc[i] = fmaf(HE, occ, gacc[i]);
+        }
+        // d / d ln K(l, i), rate i -> l: skeleton score and dwell pathwise term
+        const float Esm = sP.E[U.sm];
+#pragma unroll
+        for (int l = 0; l < NS; ++l) {
+#pragma unroll
+            for (int i = 0; i < NS; ++i) {
+                if (i == l) continue;
+                const int idx = l * (NS - 1) + (i < l ? i : i - 1);
+                int nout = 0;
+#pragma unroll
+                for (int j = 0; j < NS; ++j) nout += U.cnt[i][j];
+                const float pj = sP.pj[i * 4 + l];
+                float score = sP.dlnpi[U.s0 * 12 + idx] + (float)U.cnt[i][l] - (float)nout * pj;
+                float path = -pj * U.D[i] * (sP.E[i] - Esm) * invT;
+                gacc[NS + idx] = fmaf(WG, score, fmaf(HE, path, gacc[NS + idx]));
+            }
+        }
+    }
+    if (lim) atomicAdd(a.limit_hits, (unsigned long long)lim);
+#pragma unroll
+    for (int k = 0; k < NG; ++k) s_red[k][tid] = gacc[k];
+    __syncthreads();
+    const int warp = tid >> 5, lane = tid & 31;
+    double *out = a.gpart + ((size_t)p * a.nblk + blockIdx.x) * kExpGrad;
+    for (int k = warp; k < NG; k += kExpThreads / 32) {
+        double v = warp_sum_fixed(&s_red[k][0], lane);
+        if (lane == 0) out[k] = v;
+    }
+}
+
+__global__ void exp_grad_kernel(const ExpArgs a) {
+    const int p = blockIdx.x;
+    const int k = threadIdx.x;
+    const int ng = a.n + a.n * (a.n - 1);
+    if (k >= ng) return;
+    const double *src = a.gpart + (size_t)p * a.nblk * kExpGrad + k;
+    double v = 0.0;
+    for (int j = 0; j < a.nblk; ++j) v += src[(size_t)j * kExpGrad];
+    const double up = a.dchi2 ? a.dchi2[p] : 1.0;
+    a.grad[(size_t)p * kExpGrad + k] = v * up;
+}
+
+__global__ void inv_table_kernel(float *inv) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < kExpInvN) inv[k] = k > 0 ? 1.0f / (float)k : 0.0f;
+}
+
+template <int NS>
+cudaError_t fwd_n(const ExpArgs &a, cudaStream_t st) {
+    const size_t dyn = sizeof(float) * (size_t)a.nbins * kExpThreads;
+    cudaError_t e = cudaFuncSetAttribute(exp_fwd_kernel<NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+    if (e != cudaSuccess) return e;
+    exp_fwd_kernel<NS><<<dim3(a.nblk, a.P), kExpThreads, dyn, st>>>(a);
+    return cudaGetLastError();
+}
+
+template <int NS>
+cudaError_t adj_n(const ExpArgs &a, cudaStream_t st) {
+    exp_adj_kernel<NS><<<dim3(a.nblk, a.P), kExpThreads, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_exp_forward(const ExpArgs &a, cudaStream_t st) {
+    cudaError_t e;
+    switch (a.n) {
+    case 1: e = fwd_n<1>(a, st); break;
+    case 2: e = fwd_n<2>(a, st); break;
+    case 3: e = fwd_n<3>(a, st); break;
+    case 4: e = fwd_n<4>(a, st); break;
+    default: return cudaErrorInvalidValue;
+    }
+    if (e != cudaSuccess) return e;
+    exp_chi2_kernel<<<a.P, kExpMaxBins, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_exp_adjoint(const ExpArgs &a, cudaStream_t st) {
+    cudaError_t e;
+    switch (a.n) {
+    case 1: e = adj_n<1>(a, st); break;
+    case 2: e = adj_n<2>(a, st); break;
+    case 3: e = adj_n<3>(a, st); break;
+    case 4: e = adj_n<4>(a, st); break;
+    default: return cudaErrorInvalidValue;
+    }
+    if (e != cudaSuccess) return e;
+    exp_grad_kernel<<<a.P, 32, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_exp_inv_table(float *inv, cudaStream_t st) {
+    inv_table_kernel<<<(kExpInvN + 255) / 256, 256, 0, st>>>(inv);
+    return cudaGetLastError();
+}
+
+// Blocks per parameter set: about two waves of the device over all sets,
+// and no more than the units need.
+int exp_blocks_per_param(int P, int64_t units, int num_sms) {
+    int64_t want = (int64_t)num_sms * 6 / std::max(1, P);
+    int64_t need = (units + kExpThreads - 1) / kExpThreads;
+    return (int)std::max<int64_t>(1, std::min(want, need));
+}
+
+}  // namespace gpda

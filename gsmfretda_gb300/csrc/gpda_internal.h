@@ -109,4 +109,59 @@ cudaError_t pda_set_smem_limit(int mode, size_t dyn_smem);
 // host parameter derivation (gpda_params.cpp)
 int build_params(int n, const float *args, float gamma, float ct, bool need_pi, DevParams *out);
 
+// ---------------------------------------------------------------- expected histogram
+// Differentiable expected-histogram form of the occupancy model. A unit's
+// state skeleton (initial state, jump targets) is drawn from the fixed Philox
+// uniforms under an anchor parameter set theta0; its dwells are
+// -ln(u) / k_exit(s; theta) (reparameterised), and the skeleton carries the
+// likelihood-ratio weight W = pi_theta(s0)/pi_theta0(s0) * prod
+// P_theta(s_k|s_k-1)/P_theta0(s_k|s_k-1), so that the result is smooth in
+// theta and W = 1 at theta = theta0. The binomial split is replaced by its
+// bin masses.
+constexpr int kExpMaxStates = 4;
+constexpr int kExpMaxBins = 64;
+constexpr int kExpGrad = 16;        // n + n(n-1) <= 16 gradient components
+constexpr int kExpInvN = 4096;      // 1/k table for the binomial recurrence
+struct ExpParams {                  // 128 words
+    int32_t n, pad_[3];
+    float E[4];
+    float kexit[4];                 // theta: exit rates
+    float inv_kexit[4];             // theta
+    float init_cdf[4];              // theta0: cumulative stationary distribution
+    float jump_cdf[16];             // theta0: cumulative jump probabilities [from*4 + to]
+    float lw_init[4];               // ln pi_theta(s) - ln pi_theta0(s)
+    float lw_jump[16];              // ln P_theta(to|from) - ln P_theta0(to|from)
+    float pj[16];                   // P_theta(to|from)
+    float dlnpi[48];                // d ln pi_theta(s) / d ln K_idx  [s*12 + idx]
+    float pad2_[8];
+};
+static_assert(sizeof(ExpParams) == 128 * 4, "ExpParams layout");
+
+struct ExpArgs {
+    const int32_t *N;
+    const float *T;
+    const ExpParams *params;        // [P]
+    const float *obs;               // [nbins]
+    const float *inv;               // [kExpInvN] 1/k
+    double *part;                   // [P][nblk][nbins]   forward partial sums
+    double *hist;                   // [P][nbins]         expected counts (sum over samples)
+    double *chi2;                   // [P]
+    float *g;                       // [P][nbins]         d chi2 / d hist
+    double *gpart;                  // [P][nblk][kExpGrad]
+    double *grad;                   // [P][kExpGrad]      [dE(n), dlnK(n(n-1))]
+    const double *dchi2;            // [P] upstream gradient, null = 1
+    unsigned long long *limit_hits;
+    int64_t B;
+    int32_t S, P, nbins, left_pad, nblk, n;
+    uint64_t seed;
+    float gamma, ct, bg_a, bg_d;
+};
+
+cudaError_t launch_exp_forward(const ExpArgs &a, cudaStream_t st);
+cudaError_t launch_exp_adjoint(const ExpArgs &a, cudaStream_t st);
+cudaError_t launch_exp_inv_table(float *inv, cudaStream_t st);
+int exp_blocks_per_param(int P, int64_t units, int num_sms);
+int build_exp_params(int n, const float *theta, const float *anchor, float gamma, float ct,
+                     ExpParams *out);
+
 }  // namespace gpda

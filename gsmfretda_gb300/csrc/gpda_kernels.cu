@@ -25,22 +25,6 @@
 
 namespace gpda {
 
-__device__ __forceinline__ int cat_draw(const float *cdf, int n, float u) {
-    for (int i = 0; i < n; ++i)
-        if (u <= cdf[i]) return i;
-    return n - 1;
-}
-
-__device__ __forceinline__ int jump_draw(const float *row, int n, int from, float u) {
-    int last = from;
-    for (int i = 0; i < n; ++i) {
-        if (i == from) continue;
-        last = i;
-        if (u <= row[i]) return i;
-    }
-    return last;
-}
-
 // number of offsets < x in the sorted range a[lo, hi)
 __device__ __forceinline__ int lower_bound(const float *a, int lo, int hi, float x) {
     while (lo < hi) {
@@ -85,24 +69,6 @@ __device__ __forceinline__ void unit_begin(Unit &U, int u, int S, int64_t tb0, c
 __device__ __forceinline__ int next_state(const Unit &U, const DevParams &P, float us) {
     return (U.seg == 0) ? cat_draw(P.init_cdf, P.n, us)
                         : jump_draw(P.jump_cdf + U.st * 8, P.n, U.st, us);
-}
-
-// Background of one window (Poisson, clipped as draw_P_B_Tr does,
-// src/gen_rand.cuh:92-107), acceptor channel first; returns the acceptor
-// background, writes the remaining signal photons to *sig.
-__device__ __forceinline__ int background(Rng &r, int navail, float lam_a, float lam_d, int *sig,
-                                          int &lim, const float *inv) {
-    int B[2];
-    int avail = navail;
-#pragma unroll
-    for (int c = 0; c < 2; ++c) {
-        int x = poisson(r, c == 0 ? lam_a : lam_d, lim, inv);
-        if (x > avail) x = (int)floorf((float)avail * r.u01());
-        B[c] = x;
-        avail -= x;
-    }
-    *sig = avail;
-    return B[0];
 }
 
 // Binomial(n, eps) of a photon-mode segment (eps = eps_state, V_state = 0):

@@ -170,4 +170,117 @@ int build_params(int n, const float *args, float gamma, float ct, bool need_pi, 
     return 0;
 }
 
+// ---------------------------------------------------------------- expected histogram
+
+namespace {
+
+// Rate matrix of a parameter vector in FP64, column-major K[j*n + i] = rate j->i,
+// diagonal = -exit rate.
+void rate_matrix(int n, const float *args, double *K, double *kexit, double *kmax) {
+    const float *ko = args + n;
+    *kmax = 1.0;
+    for (int j = 0; j < n; ++j) {
+        double colsum = 0.0;
+        for (int i = 0; i < n; ++i) {
+            if (i == j) continue;
+            double k = (double)koff(ko, n, i, j);
+            K[j * n + i] = k;
+            colsum += k;
+            if (k > *kmax) *kmax = k;
+        }
+        K[j * n + j] = -colsum;
+        kexit[j] = colsum;
+    }
+}
+
+// Solves rows 0..n-2 of K x = r together with sum(x) = r[n-1] (the balance
+// equations with the last one replaced by the normalisation), Gaussian
+// elimination with partial pivoting. Returns -2 when the system is singular.
+int solve_balance(int n, const double *K, const double *r, double kmax, double *x) {
+    double A[kExpMaxStates][kExpMaxStates + 1];
+    for (int i = 0; i < n; ++i) {
+        for (int j = 0; j < n; ++j) A[i][j] = (i == n - 1) ? 1.0 : K[j * n + i];
+        A[i][n] = r[i];
+    }
+    for (int c = 0; c < n; ++c) {
+        int piv = c;
+        for (int q = c + 1; q < n; ++q)
+            if (std::fabs(A[q][c]) > std::fabs(A[piv][c])) piv = q;
+        if (!(std::fabs(A[piv][c]) > 1e-13 * kmax)) return -2;
+        if (piv != c)
+            for (int k = 0; k <= n; ++k) { double t = A[c][k]; A[c][k] = A[piv][k]; A[piv][k] = t; }
+        for (int q = c + 1; q < n; ++q) {
+            double f = A[q][c] / A[c][c];
+            for (int k = c; k <= n; ++k) A[q][k] = A[q][k] - f * A[c][k];
+        }
+    }
+    for (int q = n - 1; q >= 0; --q) {
+        double v = A[q][n];
+        for (int k = q + 1; k < n; ++k) v = v - A[q][k] * x[k];
+        x[q] = v / A[q][q];
+    }
+    return 0;
+}
+
+int stationary(int n, const double *K, double kmax, double *pi) {
+    double r[kExpMaxStates] = {0.0, 0.0, 0.0, 0.0};
+    r[n - 1] = 1.0;
+    if (solve_balance(n, K, r, kmax, pi)) return -2;
+    for (int i = 0; i < n; ++i)
+        if (!(pi[i] > 0.0)) return -2;
+    return 0;
+}
+
+}  // namespace
+
+int build_exp_params(int n, const float *theta, const float *anchor, float gamma, float ct,
+                     ExpParams *out) {
+    std::memset(out, 0, sizeof(*out));
+    if (n < 1 || n > kExpMaxStates || theta == nullptr || anchor == nullptr) return -1;
+    DevParams dt, d0;
+    int rc = build_params(n, theta, gamma, ct, true, &dt);
+    if (rc) return rc;
+    rc = build_params(n, anchor, gamma, ct, true, &d0);
+    if (rc) return rc;
+    if (dt.anyV || d0.anyV) return -1;      // no distance broadening in this form
+    double Kt[16], K0[16], kt[4], k0[4], kmt, km0, pit[4], pi0[4];
+    rate_matrix(n, theta, Kt, kt, &kmt);
+    rate_matrix(n, anchor, K0, k0, &km0);
+    if (stationary(n, Kt, kmt, pit) || stationary(n, K0, km0, pi0)) return -2;
+    out->n = n;
+    const float ninf = -INFINITY;
+    for (int i = 0; i < n; ++i) {
+        out->E[i] = dt.E[i];
+        out->kexit[i] = dt.kexit[i];
+        out->inv_kexit[i] = dt.inv_kexit[i];
+        out->init_cdf[i] = d0.init_cdf[i];
+        out->lw_init[i] = (float)(std::log(pit[i]) - std::log(pi0[i]));
+        for (int l = 0; l < n; ++l) {
+            out->jump_cdf[i * 4 + l] = d0.jump_cdf[i * 8 + l];
+            if (l == i) continue;
+            double pt = kt[i] > 0.0 ? Kt[i * n + l] / kt[i] : 0.0;
+            double p0 = k0[i] > 0.0 ? K0[i * n + l] / k0[i] : 0.0;
+            out->pj[i * 4 + l] = (float)pt;
+            out->lw_jump[i * 4 + l] = (p0 > 0.0) ? (pt > 0.0 ? (float)(std::log(pt) - std::log(p0)) : ninf) : 0.0f;
+        }
+    }
+    // d pi / d ln K(i,j) (rate j->i): K dpi = -dK pi with dK = K(i,j) (e_i - e_j) e_j^T,
+    // sum(dpi) = 0.
+    for (int i = 0; i < n; ++i) {
+        for (int j = 0; j < n; ++j) {
+            if (i == j) continue;
+            const int idx = i * (n - 1) + (j < i ? j : j - 1);
+            double r[kExpMaxStates] = {0.0, 0.0, 0.0, 0.0};
+            const double f = Kt[j * n + i] * pit[j];
+            r[i] -= f;
+            r[j] += f;
+            r[n - 1] = 0.0;
+            double dpi[kExpMaxStates];
+            if (solve_balance(n, Kt, r, kmt, dpi)) return -2;
+            for (int s2 = 0; s2 < n; ++s2) out->dlnpi[s2 * 12 + idx] = (float)(dpi[s2] / pit[s2]);
+        }
+    }
+    return 0;
+}
+
 }  // namespace gpda

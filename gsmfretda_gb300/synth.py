@@ -117,6 +117,31 @@ def photon_3state(B=100000, seed=2, with_offsets=True):
     return bs, 3, args, dict(MODEL_DEFAULTS), 100
 
 
+def expected_bursts(B=20000, n=3, seed=4):
+    """Differentiable expected-histogram workload: bursts as photon_3state
+    (N = 30 + Geometric(mean 120), T lognormal around 1.5 ms) without offsets,
+    64 fixed-uniform dwell samples per burst; n = 2 uses occupancy_2state's
+    parameters, n = 3 random_3state_args."""
+    bs, _, args3, md, _ = photon_3state(B=B, seed=seed, with_offsets=False)
+    if n == 2:
+        args = pack_args([0.30, 0.72], np.array([[0.0, 500.0], [500.0, 0.0]]))
+    elif n == 3:
+        args = args3
+    else:
+        raise ValueError("expected_bursts: n is 2 or 3")
+    return bs, n, args, md, 64
+
+
+def perturb_args(args, n, dE=0.05, dlogk=0.3, seed=0):
+    """A nearby parameter vector: E shifted (clipped to [0.02, 0.98]) and the
+    off-diagonal rates scaled by exp(+-dlogk)."""
+    rng = np.random.default_rng(seed)
+    a = np.array(args, dtype=np.float64).copy()
+    a[:n] = np.clip(a[:n] + rng.uniform(-dE, dE, n), 0.02, 0.98)
+    a[n:n * n] = a[n:n * n] * np.exp(rng.uniform(-dlogk, dlogk, n * n - n))
+    return a.astype(np.float32)
+
+
 def population_args(P, seed, n=2):
     rng = np.random.default_rng(seed)
     out = []

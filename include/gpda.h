@@ -151,6 +151,36 @@ float gpda_kernel_ms(gpda_ctx *ctx);
 /* Number of units whose segment/rejection loops hit their bound so far. */
 int64_t gpda_limit_hits(gpda_ctx *ctx);
 
+/* ---- Differentiable expected histogram (occupancy model), no counterpart
+ * in the reference: the gradient path of the parameter-server side.
+ *
+ * Each unit (parameter set p, burst b, dwell sample s < samples) draws its
+ * state skeleton and background counts from the same Philox counters as the
+ * sampled occupancy model (pword = p), with the skeleton taken from `anchor`
+ * (NULL = params) and dwells -ln(u)/k_exit(state; params); the skeleton is
+ * weighted by the likelihood ratio of params to anchor (1 when they are
+ * equal). The binomial split is replaced by its bin masses, so hist_out
+ * (P*nbins, nullable) holds expected counts summed over samples and chi2_out
+ * (P) the reduced chi-square against the observed histogram in the same form
+ * as gpda_run_plain. Parameter vectors as gpda_run_batched with V = 0;
+ * n_states <= 4 and nbins <= 64 (GPDA_ERR_LIMIT beyond). Synchronous. */
+int32_t gpda_expected_hist(gpda_ctx *ctx, int32_t P, int32_t n_states, const float *params,
+                           const float *anchor, int32_t samples, uint64_t seed,
+                           double *hist_out, double *chi2_out);
+/* Gradient of dchi2[p] * chi2[p] (dchi2 NULL = 1) with respect to E (dE,
+ * P*n) and to the natural logarithm of the off-diagonal rates in parameter
+ * order (dlogK, P*n(n-1)), at the same arguments as the preceding
+ * gpda_expected_hist on this context (the forward is re-run when they differ).
+ * The derivative is pathwise for dwells and E and likelihood-ratio for the
+ * skeleton. Synchronous. */
+int32_t gpda_expected_hist_adjoint(gpda_ctx *ctx, int32_t P, int32_t n_states,
+                                   const float *params, const float *anchor, int32_t samples,
+                                   uint64_t seed, const double *dchi2, double *dE, double *dlogK);
+/* Forward and gradient (dchi2 = 1) in one call, one synchronisation. */
+int32_t gpda_expected_grad(gpda_ctx *ctx, int32_t P, int32_t n_states, const float *params,
+                           const float *anchor, int32_t samples, uint64_t seed, double *hist_out,
+                           double *chi2_out, double *dE, double *dlogK);
+
 /* No counterpart in the reference. For callers that cannot allocate device
  * memory where they evaluate parameter sets (e.g. a framework whose caching
  * allocator owns the device memory, or a loop that must not pay cudaMalloc's

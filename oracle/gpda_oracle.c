@@ -645,3 +645,295 @@ void orc_bin_values(const float *x, int64_t n, int32_t nbins, float *hist_out) {
         if (b >= 0) hist_out[b] += 1.0f;
     }
 }
+
+/* ------------------------------------------------------------------ */
+/* Differentiable expected histogram (occupancy form), FP64 restatement of
+ * gpda_expected_hist / gpda_expected_hist_adjoint.
+ *
+ * The state skeleton comes from the FP32 mirror (anchor tables, same Philox
+ * counters and draw order as unit_occ); the background counts too, but from
+ * counter block 2^31 on (independent of the trajectory's length). Both are the
+ * device's integers. Everything continuous is FP64: dwells
+ * -ln(u)/k_exit(theta), the likelihood-ratio weight, E_eff, the binomial
+ * masses (exact over all x from a log-factorial table, no truncation), the
+ * chi-square and the gradient. d ln pi / d ln K is a central difference of
+ * the FP64 stationary solve (independent of the device's linear solve). */
+
+#define XMAXS 4
+
+typedef struct {
+    int n;
+    double E[XMAXS], kexit[XMAXS];
+    double pi[XMAXS], pj[XMAXS][XMAXS];      /* theta */
+    double lw_init[XMAXS], lw_jump[XMAXS][XMAXS];
+    double dlnpi[XMAXS][XMAXS * (XMAXS - 1)];
+} x_par;
+
+/* K (column-major, K[j*n+i] = rate j->i) from a parameter vector, with the
+ * off-diagonal `pidx` (parameter order) scaled by exp(h). */
+static void x_rates(int n, const float *args, int pidx, double h, double *K, double *kexit) {
+    const float *ko = args + n;
+    for (int j = 0; j < n; ++j) {
+        double cs = 0.0;
+        for (int i = 0; i < n; ++i) {
+            if (i == j) continue;
+            int idx = i * (n - 1) + (j < i ? j : j - 1);
+            double k = (double)koff_at(ko, n, i, j);
+            if (idx == pidx) k *= exp(h);
+            K[j * n + i] = k;
+            cs += k;
+        }
+        K[j * n + j] = -cs;
+        kexit[j] = cs;
+    }
+}
+
+static int x_pi(int n, const double *K, double *pi) {
+    double A[XMAXS][XMAXS + 1];
+    for (int i = 0; i < n; ++i) {
+        for (int j = 0; j < n; ++j) A[i][j] = (i == n - 1) ? 1.0 : K[j * n + i];
+        A[i][n] = (i == n - 1) ? 1.0 : 0.0;
+    }
+    for (int c = 0; c < n; ++c) {
+        int piv = c;
+        for (int r = c + 1; r < n; ++r) if (fabs(A[r][c]) > fabs(A[piv][c])) piv = r;
+        if (!(fabs(A[piv][c]) > 0.0)) return -2;
+        if (piv != c) for (int k = 0; k <= n; ++k) { double t = A[c][k]; A[c][k] = A[piv][k]; A[piv][k] = t; }
+        for (int r = c + 1; r < n; ++r) {
+            double f = A[r][c] / A[c][c];
+            for (int k = c; k <= n; ++k) A[r][k] -= f * A[c][k];
+        }
+    }
+    for (int r = n - 1; r >= 0; --r) {
+        double s = A[r][n];
+        for (int k = r + 1; k < n; ++k) s -= A[r][k] * pi[k];
+        pi[r] = s / A[r][r];
+    }
+    for (int i = 0; i < n; ++i) if (!(pi[i] > 0.0)) return -2;
+    return 0;
+}
+
+static int x_build(int n, const float *theta, const float *anchor, x_par *xp) {
+    double Kt[16], K0[16], kt[4], k0[4], pi0[4];
+    for (int i = 0; i < n; ++i)
+        if (theta[n * n + i] != 0.0f || anchor[n * n + i] != 0.0f) return -1;
+    x_rates(n, theta, -1, 0.0, Kt, kt);
+    x_rates(n, anchor, -1, 0.0, K0, k0);
+    if (x_pi(n, Kt, xp->pi) || x_pi(n, K0, pi0)) return -2;
+    xp->n = n;
+    for (int i = 0; i < n; ++i) {
+        xp->E[i] = (double)theta[i];
+        xp->kexit[i] = kt[i];
+        xp->lw_init[i] = log(xp->pi[i]) - log(pi0[i]);
+        for (int l = 0; l < n; ++l) {
+            xp->pj[i][l] = 0.0;
+            xp->lw_jump[i][l] = 0.0;
+            if (l == i) continue;
+            double pt = kt[i] > 0.0 ? Kt[i * n + l] / kt[i] : 0.0;
+            double p0 = k0[i] > 0.0 ? K0[i * n + l] / k0[i] : 0.0;
+            xp->pj[i][l] = pt;
+            if (p0 > 0.0) xp->lw_jump[i][l] = pt > 0.0 ? log(pt) - log(p0) : -INFINITY;
+        }
+    }
+    const double h = 1e-6;
+    for (int idx = 0; idx < n * (n - 1); ++idx) {
+        double Kp[16], Km[16], kk[4], pp[4], pm[4];
+        x_rates(n, theta, idx, h, Kp, kk);
+        x_rates(n, theta, idx, -h, Km, kk);
+        if (x_pi(n, Kp, pp) || x_pi(n, Km, pm)) return -2;
+        for (int s = 0; s < n; ++s) xp->dlnpi[s][idx] = (log(pp[s]) - log(pm[s])) / (2.0 * h);
+    }
+    return 0;
+}
+
+typedef struct {
+    double eeff, W, dtl, D[XMAXS];
+    int s0, sm, cnt[XMAXS][XMAXS], sig, ba, timed;
+} x_unit;
+
+/* one unit: skeleton from the FP32 anchor tables, FP64 dwells under theta */
+static int x_walk(const f32_tab *sk, const x_par *xp, int Nb, float Tb, float bga, float bgd,
+                  uint64_t seed, uint32_t pw, uint32_t b, uint32_t s, x_unit *U) {
+    if (Nb <= 0) return 0;
+    orc_rng r;
+    rng_init(&r, seed, pw, b, s);
+    int n = xp->n, st = 0;
+    double t = 0.0, acc = 0.0, lw = 0.0, T = (double)Tb;
+    memset(U, 0, sizeof(*U));
+    U->timed = Tb > 0.0f;
+    for (int seg = 0; seg < ORC_MAX_SEG; ++seg) {
+        float us = f32_u01(&r);
+        int ns;
+        if (seg == 0) {
+            ns = f32_cat(sk->init_cdf, n, us);
+            U->s0 = ns;
+            lw += xp->lw_init[ns];
+        } else {
+            ns = f32_jump(sk->jump_cdf + st * ORC_MAXS, n, st, us);
+            lw += xp->lw_jump[st][ns];
+            U->cnt[st][ns] += 1;
+        }
+        st = ns;
+        if (!U->timed) break;
+        float u = f32_u01(&r);
+        double tau = xp->kexit[st] > 0.0 ? -log((double)u) / xp->kexit[st] : INFINITY;
+        double tn = t + tau;
+        int last = !(tn < T) || seg == ORC_MAX_SEG - 1;
+        double dt = last ? T - t : tau;
+        acc += dt * xp->E[st];
+        if (last) { U->dtl = dt; break; }
+        U->D[st] += dt;
+        t = tn;
+    }
+    U->sm = st;
+    U->eeff = U->timed ? acc / T : xp->E[st];
+    U->W = exp(lw);
+    r.ctr[0] = 0x80000000u;        /* background from a fixed counter block */
+    rng_align(&r);
+    int Ba = f32_poisson(&r, bga * Tb);
+    if (Ba > Nb) Ba = (int)floorf((float)Nb * f32_u01(&r));
+    int rem = Nb - Ba;
+    int Bd = f32_poisson(&r, bgd * Tb);
+    if (Bd > rem) Bd = (int)floorf((float)rem * f32_u01(&r));
+    U->ba = Ba;
+    U->sig = rem - Bd;
+    return 1;
+}
+
+static inline double x_eps(double e, double g, double ct) {
+    double om = 1.0 - e, num = g * e + ct * om;
+    return num / (num + om);
+}
+static inline double x_deps(double e, double g, double ct) {
+    double om = 1.0 - e, num = g * e + ct * om, den = num + om;
+    return ((g - ct) * om + num) / (den * den);
+}
+
+/* visits every x of Binomial(sig, p): fn(bin, P(x), x) */
+#define X_FOR_MASSES(U, Nb, nbins, p, lf, BODY)                                               \
+    do {                                                                                       \
+        int sig_ = (U).sig;                                                                    \
+        if (sig_ <= 0 || !((p) > 0.0) || (p) >= 1.0) {                                        \
+            int x = (sig_ > 0 && (p) >= 1.0) ? sig_ : 0;                                       \
+            int bin = pda_bin((U).ba + x, Nb, nbins);                                          \
+            double mass = 1.0;                                                                 \
+            BODY;                                                                              \
+        } else {                                                                               \
+            double lp_ = log(p), lq_ = log1p(-(p));                                            \
+            for (int x = 0; x <= sig_; ++x) {                                                  \
+                double mass = exp(lf[sig_] - lf[x] - lf[sig_ - x] + x * lp_ + (sig_ - x) * lq_); \
+                int bin = pda_bin((U).ba + x, Nb, nbins);                                      \
+                BODY;                                                                          \
+            }                                                                                  \
+        }                                                                                      \
+    } while (0)
+
+int orc_expected(const orc_bursts *bs, int32_t n, const float *params, const float *anchor,
+                 int32_t P, const orc_model *m, int32_t S, uint64_t seed, const float *obs,
+                 double *hist, double *chi2, double *dE, double *dlogK, int32_t nthreads) {
+    init_lf_d();
+    if (n < 1 || n > XMAXS || P < 1 || S < 1 || !params || !obs || !hist || !chi2) return -1;
+    const int nb = m->nbins, nk = n * (n - 1);
+    int maxN = 0;
+    for (int64_t b = 0; b < bs->B; ++b) if (bs->N[b] > maxN) maxN = bs->N[b];
+    double *lf = (double *)malloc(sizeof(double) * (size_t)(maxN + 1));
+    if (!lf) return -4;
+    for (int k = 0; k <= maxN; ++k) lf[k] = lgamma((double)k + 1.0);
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+    const double g = m->gamma, ct = m->crosstalk;
+    const float bga = m->bg_a, bgd = m->bg_d;
+    int rc = 0;
+    for (int p = 0; p < P && rc == 0; ++p) {
+        const float *th = params + (size_t)p * n * (n + 1);
+        const float *an = anchor ? anchor + (size_t)p * n * (n + 1) : th;
+        f32_tab sk;
+        x_par xp;
+        if ((rc = f32_build(n, an, m, &sk, 1)) != 0) break;
+        if ((rc = x_build(n, th, an, &xp)) != 0) break;
+        double *H = hist + (size_t)p * nb;
+        for (int i = 0; i < nb; ++i) H[i] = 0.0;
+        /* forward */
+#pragma omp parallel
+        {
+            double loc[64];
+            for (int i = 0; i < nb; ++i) loc[i] = 0.0;
+#pragma omp for schedule(dynamic, 64)
+            for (int64_t b = 0; b < bs->B; ++b) {
+                int Nb = bs->N[b];
+                for (int s = 0; s < S; ++s) {
+                    x_unit U;
+                    if (!x_walk(&sk, &xp, Nb, bs->T[b], bga, bgd, seed, (uint32_t)p, (uint32_t)b, (uint32_t)s, &U)) continue;
+                    double pe = x_eps(U.eeff, g, ct);
+                    X_FOR_MASSES(U, Nb, nb, pe, lf, loc[bin] += U.W * mass);
+                }
+            }
+#pragma omp critical
+            for (int i = 0; i < nb; ++i) H[i] += loc[i];
+        }
+        /* chi-square and d chi2 / d hist */
+        int effN = nb - m->left_pad;
+        double chi = 0.0, gb[64];
+        for (int i = m->left_pad; i < nb; ++i) {
+            if (H[i] > 0.0) {
+                double mi = H[i] / S, d = (double)obs[i] - mi;
+                chi += d * d / mi;
+            } else {
+                effN -= 1;
+            }
+        }
+        double den = (double)(effN - n * (n + 1));
+        chi2[p] = chi / den;
+        for (int i = 0; i < nb; ++i) {
+            gb[i] = 0.0;
+            if (i >= m->left_pad && H[i] > 0.0) {
+                double mi = H[i] / S, o = (double)obs[i];
+                gb[i] = (1.0 - o * o / (mi * mi)) / (S * den);
+            }
+        }
+        if (!dE && !dlogK) continue;
+        /* adjoint */
+        double gE[XMAXS] = {0}, gK[XMAXS * (XMAXS - 1)] = {0};
+#pragma omp parallel
+        {
+            double lE[XMAXS] = {0}, lK[XMAXS * (XMAXS - 1)] = {0};
+#pragma omp for schedule(dynamic, 64)
+            for (int64_t b = 0; b < bs->B; ++b) {
+                int Nb = bs->N[b];
+                for (int s = 0; s < S; ++s) {
+                    x_unit U;
+                    if (!x_walk(&sk, &xp, Nb, bs->T[b], bga, bgd, seed, (uint32_t)p, (uint32_t)b, (uint32_t)s, &U)) continue;
+                    double pe = x_eps(U.eeff, g, ct);
+                    double G = 0.0, GX = 0.0;
+                    X_FOR_MASSES(U, Nb, nb, pe, lf, { G += gb[bin] * mass; GX += gb[bin] * mass * x; });
+                    double Hd = 0.0;
+                    if (U.sig > 0 && pe > 0.0 && pe < 1.0) Hd = (GX - U.sig * pe * G) / (pe * (1.0 - pe));
+                    double HE = U.W * Hd * x_deps(U.eeff, g, ct), WG = U.W * G;
+                    double invT = U.timed ? 1.0 / (double)bs->T[b] : 0.0;
+                    for (int i = 0; i < n; ++i) {
+                        double occ = U.timed ? (U.D[i] + (i == U.sm ? U.dtl : 0.0)) * invT : (i == U.sm ? 1.0 : 0.0);
+                        lE[i] += HE * occ;
+                    }
+                    for (int l = 0; l < n; ++l)
+                        for (int i = 0; i < n; ++i) {
+                            if (i == l) continue;
+                            int idx = l * (n - 1) + (i < l ? i : i - 1);
+                            int nout = 0;
+                            for (int j = 0; j < n; ++j) nout += U.cnt[i][j];
+                            double score = xp.dlnpi[U.s0][idx] + U.cnt[i][l] - nout * xp.pj[i][l];
+                            double path = -xp.pj[i][l] * U.D[i] * (xp.E[i] - xp.E[U.sm]) * invT;
+                            lK[idx] += WG * score + HE * path;
+                        }
+                }
+            }
+#pragma omp critical
+            {
+                for (int i = 0; i < n; ++i) gE[i] += lE[i];
+                for (int k = 0; k < nk; ++k) gK[k] += lK[k];
+            }
+        }
+        if (dE) for (int i = 0; i < n; ++i) dE[(size_t)p * n + i] = gE[i];
+        if (dlogK) for (int k = 0; k < nk; ++k) dlogK[(size_t)p * nk + k] = gK[k];
+    }
+    free(lf);
+    return rc;
+}

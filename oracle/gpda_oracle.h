@@ -149,6 +149,16 @@ float orc_chi2_f32(const float *mhist, const float *ohist, int32_t nbins,
 /* Boost regular-axis binning of float values on [0,1): inner bins only */
 void orc_bin_values(const float *x, int64_t n, int32_t nbins, float *hist_out);
 
+/* Differentiable expected histogram, occupancy form (no reference
+ * counterpart; checker of gpda_expected_hist / _adjoint): FP64 except the
+ * state skeleton and background counts, which are the FP32 mirror's draws
+ * under `anchor` (NULL = params). hist: P*nbins expected counts summed over
+ * samples; chi2: P; dE (P*n) and dlogK (P*n(n-1)), nullable, the gradient of
+ * chi2 in E and ln K (parameter order). n <= 4, V = 0. */
+int orc_expected(const orc_bursts *bs, int32_t n, const float *params, const float *anchor,
+                 int32_t P, const orc_model *m, int32_t S, uint64_t seed, const float *obs,
+                 double *hist, double *chi2, double *dE, double *dlogK, int32_t nthreads);
+
 #ifdef __cplusplus
 }
 #endif

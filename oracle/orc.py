@@ -71,6 +71,10 @@ def lib():
         _lib.orc_run_refcompat.argtypes = [C.POINTER(OrcRcBursts), C.c_int32, C.c_void_p,
                                            C.POINTER(OrcModel), C.c_int32, C.c_uint64, C.c_int64,
                                            C.c_int64, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32]
+        _lib.orc_expected.argtypes = [C.POINTER(OrcBursts), C.c_int32, C.c_void_p, C.c_void_p,
+                                      C.c_int32, C.POINTER(OrcModel), C.c_int32, C.c_uint64,
+                                      C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                      C.c_int32]
         _lib.orc_bin_values.argtypes = [C.c_void_p, C.c_int64, C.c_int32, C.c_void_p]
         _lib.orc_philox4x32_10.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
     return _lib
@@ -187,3 +191,24 @@ def bin_values(x, nbins):
     h = np.zeros(nbins, dtype=np.float32)
     lib().orc_bin_values(_ptr(x), x.size, nbins, _ptr(h))
     return h
+
+
+def expected(N, T, n, args, m, S, seed, obs, anchor=None, grad=True, nthreads=0):
+    """FP64 expected-histogram forward (+ gradient): hist (P, nbins), chi2 (P,),
+    dE (P, n), dlnK (P, n(n-1)); the state skeleton is drawn under anchor."""
+    N = np.ascontiguousarray(N, dtype=np.int32)
+    T = np.ascontiguousarray(T, dtype=np.float32)
+    a = np.ascontiguousarray(args, dtype=np.float32).reshape(-1)
+    P = a.size // (n * (n + 1))
+    an = None if anchor is None else np.ascontiguousarray(anchor, dtype=np.float32).reshape(-1)
+    o = np.ascontiguousarray(obs, dtype=np.float32)
+    bs = OrcBursts(N.size, _ptr(N), _ptr(T), None, None)
+    hist = np.zeros((P, m.nbins), dtype=np.float64)
+    chi2 = np.zeros(P, dtype=np.float64)
+    dE = np.zeros((P, n), dtype=np.float64) if grad else None
+    dK = np.zeros((P, n * (n - 1)), dtype=np.float64) if grad else None
+    rc = lib().orc_expected(C.byref(bs), n, _ptr(a), _ptr(an), P, C.byref(m), S, seed, _ptr(o),
+                            _ptr(hist), _ptr(chi2), _ptr(dE), _ptr(dK), nthreads)
+    if rc != 0:
+        raise ValueError(f"orc_expected rc={rc}")
+    return hist, chi2, dE, dK
