@@ -256,7 +256,8 @@ int exp_prepare(gpda_ctx *c, int P, int n, const float *params, const float *anc
     CK(cudaSetDevice(c->device));
     CK(cudaStreamSynchronize(c->stream));   // pinned staging and scratch are free
     const int nb = c->model.nbins;
-    const int nblk = exp_blocks_per_param(P, c->B * (int64_t)S, c->num_sms);
+    int nblk = 1, nblk_adj = 1;
+    CK(exp_grid(n, nb, P, c->B * (int64_t)S, c->num_sms, &nblk, &nblk_adj));
     if (!c->dExpInv) {
         CK(cudaMalloc(&c->dExpInv, sizeof(float) * kExpInvN));
         CK(launch_exp_inv_table(c->dExpInv, c->stream));
@@ -280,7 +281,7 @@ int exp_prepare(gpda_ctx *c, int P, int n, const float *params, const float *anc
         CK(cudaMallocHost(&c->hExpOut, sizeof(double) * (size_t)P * (2 + kExpMaxBins + kExpGrad)));
         c->cap_exp_out = P;
     }
-    const size_t parts = (size_t)P * nblk;
+    const size_t parts = (size_t)P * std::max(nblk, nblk_adj);
     if (parts > c->cap_exp_part) {
         free_dev(c->dExpPart); free_dev(c->dExpGPart);
         c->dExpPart = nullptr; c->dExpGPart = nullptr; c->cap_exp_part = 0;
@@ -317,6 +318,7 @@ int exp_prepare(gpda_ctx *c, int P, int n, const float *params, const float *anc
     a.nbins = nb;
     a.left_pad = c->model.left_pad;
     a.nblk = nblk;
+    a.nblk_adj = nblk_adj;
     a.n = n;
     a.seed = seed;
     a.gamma = c->model.gamma;

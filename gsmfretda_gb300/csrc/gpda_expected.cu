@@ -49,8 +49,19 @@ __device__ __forceinline__ float log1m_(float x) {
     return logf_(1.0f - x);
 }
 
+// 1/(2j+1), j = 1..15, for the bd0 series
+__device__ __forceinline__ float inv_odd(int j) {
+    switch (j) {
+    case 1: return 0x1.555556p-2f;  case 2: return 0x1.99999ap-3f;  case 3: return 0x1.24924ap-3f;
+    case 4: return 0x1.c71c72p-4f;  case 5: return 0x1.745d18p-4f;  case 6: return 0x1.3b13b2p-4f;
+    case 7: return 0x1.111112p-4f;  case 8: return 0x1.e1e1e2p-5f;  case 9: return 0x1.af286cp-5f;
+    case 10: return 0x1.861862p-5f; case 11: return 0x1.642c86p-5f; case 12: return 0x1.47ae14p-5f;
+    case 13: return 0x1.2f684cp-5f; case 14: return 0x1.1a7b96p-5f; default: return 0x1.084210p-5f;
+    }
+}
+
 // Loader's deviance term bd0(x, np) = x ln(x / np) + np - x, by its series
-// when x is close to np.
+// sum_j 2 x v^(2j+1) / (2j+1), v = (x - np)/(x + np), when x is close to np.
 __device__ __forceinline__ float bd0(float x, float np) {
     float d = x - np;
     if (fabsf(d) < 0.1f * (x + np)) {
@@ -60,7 +71,7 @@ __device__ __forceinline__ float bd0(float x, float np) {
         float v2 = v * v;
         for (int j = 1; j < 16; ++j) {
             ej = ej * v2;
-            float s1 = s + ej / (float)(2 * j + 1);
+            float s1 = fmaf(ej, inv_odd(j), s);
             if (s1 == s) return s1;
             s = s1;
         }
@@ -69,10 +80,25 @@ __device__ __forceinline__ float bd0(float x, float np) {
     return x * logf_(x / np) + np - x;
 }
 
-// stirlerr(k) = ln k! - (k + 1/2) ln k + k - ln(2 pi)/2 = fc(k - 1), k >= 1
-__device__ __forceinline__ float stirlerr(int k) { return fc((float)(k - 1)); }
+// stirlerr(k) = ln k! - (k + 1/2) ln k + k - ln(2 pi)/2, k >= 1: exact values
+// for k <= 15, the asymptotic series 1/12k - 1/360k^3 + 1/1260k^5 - 1/1680k^7
+// beyond (truncation below 1e-13)
+__device__ __forceinline__ float stirlerr(int k) {
+    switch (k) {
+    case 1: return 0x1.4c071cp-4f;  case 2: return 0x1.52a9bap-5f;  case 3: return 0x1.c579a2p-6f;
+    case 4: return 0x1.54a266p-6f;  case 5: return 0x1.10b4e6p-6f;  case 6: return 0x1.c6b168p-7f;
+    case 7: return 0x1.85d4d6p-7f;  case 8: return 0x1.552806p-7f;  case 9: return 0x1.2f4872p-7f;
+    case 10: return 0x1.10f9d4p-7f; case 11: return 0x1.f05930p-8f; case 12: return 0x1.c70188p-8f;
+    case 13: return 0x1.a40514p-8f; case 14: return 0x1.86076cp-8f; case 15: return 0x1.6c08f6p-8f;
+    default: {
+        float r = 1.0f / (float)k;
+        float r2 = r * r;
+        return r * (0.0833333358f - r2 * (0.00277777785f - r2 * (0.000793650805f - r2 * 0.000595238095f)));
+    }
+    }
+}
 
-// P(X = m) for X ~ Binomial(n, p), 0 < p < 1, q = 1 - p
+// P(X = m) for X ~ Binomial(n, p), 0 < p < 1, q = 1 - p (Loader's form)
 __device__ __forceinline__ float binom_pmf(int n, int m, float p, float q) {
     if (m == 0) return expf_((float)n * log1m_(p));
     if (m == n) return expf_((float)n * log1m_(q));
@@ -81,10 +107,6 @@ __device__ __forceinline__ float binom_pmf(int n, int m, float p, float q) {
                bd0((float)(n - m), fn * q);
     const float inv2pi = 0.159154943091895336f;
     return expf_(lc) * sqrtf(fn * inv2pi / ((float)m * (float)(n - m)));
-}
-
-__device__ __forceinline__ float inv_of(const float *inv, int k) {
-    return (k < kExpInvN) ? __ldg(inv + k) : 1.0f / (float)k;
 }
 
 // first acceptor count a with floor(a * nbins / N) >= b
@@ -183,9 +205,11 @@ __device__ __forceinline__ float eps_dp(float e, float g, float ct) {
     return ((g - ct) * om + num) / (den * den);
 }
 
-// Walks the masses of (ba + X) / N, X ~ Binomial(sig, p), one bin run at a
-// time: F(bin, run mass, run sum of x * mass) is called once per bin touched.
-template <class F>
+// Walks the masses of (ba + X) / N, X ~ Binomial(sig, p), one bin at a
+// time, outward from the mode: F(bin, mass, sum of x * mass) is called once
+// per bin touched. Inside a bin the number of terms is known, so the term
+// loop carries no bin test; the mass cut is tested every 4 terms.
+template <bool WANT_X, class F>
 __device__ __forceinline__ void binom_bins(int Nb, int sig, int ba, float p, int nbins,
                                            const float *inv, F &&flush) {
     if (sig <= 0 || !(p > 0.0f)) {
@@ -202,49 +226,75 @@ __device__ __forceinline__ void binom_bins(int Nb, int sig, int ba, float p, int
     const float w0 = binom_pmf(sig, m, p, q);
     const float cut = w0 * kMassCut;
     const float rho = p / q, irho = q / p;
-    // upward from the mode
+    const bool tab = sig + 1 < kExpInvN;
+    // upward: x = m .. sig, ratio P(x+1)/P(x) = (sig - x) rho / (x + 1)
     {
+        int x = m;
+        float w = w0;
+        float fs = (float)(sig - m);
+        float fx = (float)m;
         int b = bin_of(ba + m, Nb, nbins);
-        int a_next = (b < nbins - 1) ? bin_start(b + 1, Nb, nbins) : 0x7fffffff;
-        float w = w0, run = 0.0f, runx = 0.0f;
-        for (int x = m; x <= sig; ++x) {
-            if (ba + x >= a_next) {
-                flush(b, run, runx);
-                run = 0.0f;
-                runx = 0.0f;
-                b = bin_of(ba + x, Nb, nbins);
-                a_next = (b < nbins - 1) ? bin_start(b + 1, Nb, nbins) : 0x7fffffff;
-            }
-            run += w;
-            runx = fmaf((float)x, w, runx);
-            if (x == sig) break;
-            w = w * ((float)(sig - x) * rho) * inv_of(inv, x + 1);
-            if (w < cut) break;
-        }
-        flush(b, run, runx);
-    }
-    // downward from the mode
-    if (m > 0) {
-        float w = w0 * ((float)m * irho) * inv_of(inv, sig - m + 1);
-        if (w >= cut) {
-            int b = bin_of(ba + m - 1, Nb, nbins);
-            int a_lo = bin_start(b, Nb, nbins);
+        bool more = true;
+        while (more) {
+            int last = (b < nbins - 1) ? bin_start(b + 1, Nb, nbins) - 1 - ba : sig;
+            if (last > sig) last = sig;
+            int cnt = last - x + 1;
             float run = 0.0f, runx = 0.0f;
-            for (int x = m - 1; x >= 0; --x) {
-                if (ba + x < a_lo) {
-                    flush(b, run, runx);
-                    run = 0.0f;
-                    runx = 0.0f;
-                    b = bin_of(ba + x, Nb, nbins);
-                    a_lo = bin_start(b, Nb, nbins);
+            while (cnt > 0) {
+                int k = cnt < 4 ? cnt : 4;
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    if (j < k) {
+                        run += w;
+                        if (WANT_X) runx = fmaf(fx, w, runx);
+                        float iv = tab ? __ldg(inv + x + 1) : 1.0f / (float)(x + 1);
+                        w = w * (fs * rho) * iv;
+                        fs -= 1.0f;
+                        fx += 1.0f;
+                        x += 1;
+                    }
                 }
-                run += w;
-                runx = fmaf((float)x, w, runx);
-                if (x == 0) break;
-                w = w * ((float)x * irho) * inv_of(inv, sig - x + 1);
-                if (w < cut) break;
+                cnt -= k;
+                if (w < cut) { more = false; break; }
             }
             flush(b, run, runx);
+            if (x > sig) more = false;
+            ++b;
+        }
+    }
+    // downward: x = m-1 .. 0, ratio P(x-1)/P(x) = x / ((sig - x + 1) rho)
+    if (m > 0) {
+        int x = m - 1;
+        float w = w0 * ((float)m * irho) * (tab ? __ldg(inv + sig - m + 1) : 1.0f / (float)(sig - m + 1));
+        if (w >= cut) {
+            float fx = (float)x;
+            int b = bin_of(ba + x, Nb, nbins);
+            bool more = true;
+            while (more) {
+                int first = bin_start(b, Nb, nbins) - ba;
+                if (first < 0) first = 0;
+                int cnt = x - first + 1;
+                float run = 0.0f, runx = 0.0f;
+                while (cnt > 0) {
+                    int k = cnt < 4 ? cnt : 4;
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) {
+                        if (j < k) {
+                            run += w;
+                            if (WANT_X) runx = fmaf(fx, w, runx);
+                            float iv = tab ? __ldg(inv + sig - x + 1) : 1.0f / (float)(sig - x + 1);
+                            w = w * (fx * irho) * iv;
+                            fx -= 1.0f;
+                            x -= 1;
+                        }
+                    }
+                    cnt -= k;
+                    if (w < cut) { more = false; break; }
+                }
+                flush(b, run, runx);
+                if (x < 0) more = false;
+                --b;
+            }
         }
     }
 }
@@ -287,7 +337,7 @@ __global__ void __launch_bounds__(kExpThreads) exp_fwd_kernel(const ExpArgs a) {
         const float eeff = (Tb > 0.0f) ? U.acc / Tb : sP.E[U.sm];
         const float W = expf_(U.lw);
         const float pe = eps_p(eeff, a.gamma, a.ct);
-        binom_bins(Nb, sig, ba, pe, a.nbins, a.inv, [&](int bin, float m, float) {
+        binom_bins<false>(Nb, sig, ba, pe, a.nbins, a.inv, [&](int bin, float m, float) {
             row[bin * kExpThreads] += W * m;
         });
     }
@@ -357,7 +407,7 @@ __global__ void __launch_bounds__(kExpThreads) exp_adj_kernel(const ExpArgs a) {
 #pragma unroll
     for (int k = 0; k < NG; ++k) gacc[k] = 0.0f;
     const int64_t units = a.B * (int64_t)a.S;
-    const int64_t stride = (int64_t)a.nblk * kExpThreads;
+    const int64_t stride = (int64_t)a.nblk_adj * kExpThreads;
     int lim = 0;
     for (int64_t u = (int64_t)blockIdx.x * kExpThreads + tid; u < units; u += stride) {
         const int b = (int)(u / a.S);
@@ -374,7 +424,7 @@ __global__ void __launch_bounds__(kExpThreads) exp_adj_kernel(const ExpArgs a) {
         const float W = expf_(U.lw);
         const float pe = eps_p(eeff, a.gamma, a.ct);
         float G = 0.0f, GX = 0.0f;
-        binom_bins(Nb, sig, ba, pe, a.nbins, a.inv, [&](int bin, float m, float mx) {
+        binom_bins<true>(Nb, sig, ba, pe, a.nbins, a.inv, [&](int bin, float m, float mx) {
             const float gb = s_g[bin];
             G = fmaf(gb, m, G);
             GX = fmaf(gb, mx, GX);
@@ -416,7 +466,7 @@ __global__ void __launch_bounds__(kExpThreads) exp_adj_kernel(const ExpArgs a) {
     for (int k = 0; k < NG; ++k) s_red[k][tid] = gacc[k];
     __syncthreads();
     const int warp = tid >> 5, lane = tid & 31;
-    double *out = a.gpart + ((size_t)p * a.nblk + blockIdx.x) * kExpGrad;
+    double *out = a.gpart + ((size_t)p * a.nblk_adj + blockIdx.x) * kExpGrad;
     for (int k = warp; k < NG; k += kExpThreads / 32) {
         double v = warp_sum_fixed(&s_red[k][0], lane);
         if (lane == 0) out[k] = v;
@@ -428,9 +478,9 @@ __global__ void exp_grad_kernel(const ExpArgs a) {
     const int k = threadIdx.x;
     const int ng = a.n + a.n * (a.n - 1);
     if (k >= ng) return;
-    const double *src = a.gpart + (size_t)p * a.nblk * kExpGrad + k;
+    const double *src = a.gpart + (size_t)p * a.nblk_adj * kExpGrad + k;
     double v = 0.0;
-    for (int j = 0; j < a.nblk; ++j) v += src[(size_t)j * kExpGrad];
+    for (int j = 0; j < a.nblk_adj; ++j) v += src[(size_t)j * kExpGrad];
     const double up = a.dchi2 ? a.dchi2[p] : 1.0;
     a.grad[(size_t)p * kExpGrad + k] = v * up;
 }
@@ -451,8 +501,18 @@ cudaError_t fwd_n(const ExpArgs &a, cudaStream_t st) {
 
 template <int NS>
 cudaError_t adj_n(const ExpArgs &a, cudaStream_t st) {
-    exp_adj_kernel<NS><<<dim3(a.nblk, a.P), kExpThreads, 0, st>>>(a);
+    exp_adj_kernel<NS><<<dim3(a.nblk_adj, a.P), kExpThreads, 0, st>>>(a);
     return cudaGetLastError();
+}
+
+template <int NS>
+cudaError_t occ_n(int nbins, int *fwd, int *adj) {
+    const size_t dyn = sizeof(float) * (size_t)nbins * kExpThreads;
+    cudaError_t e = cudaFuncSetAttribute(exp_fwd_kernel<NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+    if (e != cudaSuccess) return e;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(fwd, exp_fwd_kernel<NS>, kExpThreads, dyn);
+    if (e != cudaSuccess) return e;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(adj, exp_adj_kernel<NS>, kExpThreads, 0);
 }
 
 }  // namespace
@@ -490,12 +550,29 @@ cudaError_t launch_exp_inv_table(float *inv, cudaStream_t st) {
     return cudaGetLastError();
 }
 
-// Blocks per parameter set: about two waves of the device over all sets,
-// and no more than the units need.
-int exp_blocks_per_param(int P, int64_t units, int num_sms) {
-    int64_t want = (int64_t)num_sms * 6 / std::max(1, P);
-    int64_t need = (units + kExpThreads - 1) / kExpThreads;
-    return (int)std::max<int64_t>(1, std::min(want, need));
+// Blocks per parameter set for each kernel: one wave of the device over all
+// parameter sets (the units are strided over the blocks of a set), and no
+// more blocks than the units need.
+cudaError_t exp_grid(int n, int nbins, int P, int64_t units, int num_sms, int *nblk_fwd,
+                     int *nblk_adj) {
+    int of = 1, oa = 1;
+    cudaError_t e;
+    switch (n) {
+    case 1: e = occ_n<1>(nbins, &of, &oa); break;
+    case 2: e = occ_n<2>(nbins, &of, &oa); break;
+    case 3: e = occ_n<3>(nbins, &of, &oa); break;
+    case 4: e = occ_n<4>(nbins, &of, &oa); break;
+    default: return cudaErrorInvalidValue;
+    }
+    if (e != cudaSuccess) return e;
+    const int64_t need = (units + kExpThreads - 1) / kExpThreads;
+    auto per = [&](int occ) {
+        int64_t want = (int64_t)num_sms * std::max(1, occ) / std::max(1, P);
+        return (int)std::max<int64_t>(1, std::min(want, need));
+    };
+    *nblk_fwd = per(of);
+    *nblk_adj = per(oa);
+    return cudaSuccess;
 }
 
 }  // namespace gpda

@@ -152,7 +152,7 @@ struct ExpArgs {
     const double *dchi2;            // [P] upstream gradient, null = 1
     unsigned long long *limit_hits;
     int64_t B;
-    int32_t S, P, nbins, left_pad, nblk, n;
+    int32_t S, P, nbins, left_pad, nblk, nblk_adj, n;
     uint64_t seed;
     float gamma, ct, bg_a, bg_d;
 };
@@ -160,7 +160,8 @@ struct ExpArgs {
 cudaError_t launch_exp_forward(const ExpArgs &a, cudaStream_t st);
 cudaError_t launch_exp_adjoint(const ExpArgs &a, cudaStream_t st);
 cudaError_t launch_exp_inv_table(float *inv, cudaStream_t st);
-int exp_blocks_per_param(int P, int64_t units, int num_sms);
+cudaError_t exp_grid(int n, int nbins, int P, int64_t units, int num_sms, int *nblk_fwd,
+                     int *nblk_adj);
 int build_exp_params(int n, const float *theta, const float *anchor, float gamma, float ct,
                      ExpParams *out);
 
