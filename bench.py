@@ -56,9 +56,14 @@ def parse():
     ap.add_argument("--impl", default="gpda", choices=["gpda", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--bursts", type=int, default=B_FULL)
-    ap.add_argument("--workload", default=WORKLOAD, choices=[WORKLOAD, "population_256", "expected_20k"],
+    ap.add_argument("--fit-bursts", type=int, default=1_000_000)
+    ap.add_argument("--fit-gens", type=int, default=80)
+    ap.add_argument("--fit-steps", type=int, default=400)
+    ap.add_argument("--workload", default=WORKLOAD,
+                    choices=[WORKLOAD, "population_256", "expected_20k", "fit_4state"],
                     help="population_256: batched population vs plain per-parameter-set launches; "
-                         "expected_20k: differentiable expected histogram, forward + adjoint")
+                         "expected_20k: differentiable expected histogram, forward + adjoint; "
+                         "fit_4state: time-to-fit, adjoint-driven Adam vs evolutionary fits")
     return ap.parse_args()
 
 
@@ -375,8 +380,100 @@ def run_expected(a):
     return 0
 
 
+def run_fit(a):
+    """Time-to-fit on the 4-state cyclic system (8 nonzero rates, E = 0.15,
+    0.4, 0.6, 0.9) with 1,000,000 Pareto-N bursts (alpha 1.8, 30-3000
+    photons, T lognormal around 2 ms): the observed histogram is one sampled
+    draw per burst at the true parameters; every fit starts from the same
+    perturbed point.
+      es_plain    separable CMA-ES, population 64, sampled chi-square (10 MC
+                  samples per burst), one launch + read-back per parameter set
+      es_batched  the same, the population in one batched launch
+      adam        Adam on the expected-histogram chi-square (16 dwell samples
+                  per burst) with the adjoint gradient
+    Yardstick (outside the timers): the expected chi-square with 32 samples at
+    an unrelated seed, evaluated on every recorded iterate. Target: the
+    yardstick value the plain evolutionary fit ends at; time-to-fit = wall time
+    until a fit first reaches it."""
+    import numpy as np
+    import torch
+
+    from gsmfretda_gb300 import build as gbuild
+    from gsmfretda_gb300 import fit, synth
+    gbuild.build()
+    from gsmfretda_gb300.api import MODE_OCCUPANCY, Engine
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    bs, n, truth, md, _ = synth.fit_4state(B=a.fit_bursts)
+    # 21 bins leave 19 - n(n+1) = -1 degrees of freedom in the reduced chi-square
+    md = dict(md, nbins=41)
+    eng = Engine(local, **md)
+    eng.upload(bs)
+    ohist, _ = eng.run_plain(MODE_OCCUPANCY, n, truth, 1, HELD_OUT_SEED)
+    eng.set_observed(ohist.astype(np.float32))
+    prob = fit.FitProblem(eng, n, truth)
+    z_true = prob.from_args(truth)[0]
+    rng = np.random.default_rng(17)
+    z0 = z_true + np.concatenate([rng.uniform(-0.4, 0.4, n), rng.uniform(-0.6, 0.6, prob.D - n)])
+
+    def yard(z):
+        return float(prob.expected(z, 32, 0x5EED, grad=False)[0][0])
+
+    # warm-up of every launch shape
+    prob.expected(z0, 16, 1)
+    prob.sampled_batched(np.stack([z0] * 64), 10, 1)
+    prob.sampled_plain(z0[None], 10, 1)
+    clocks = ClockSampler(local)
+    clocks.start()
+    runs = {}
+    clocks.mark()
+    runs["es_plain"] = fit.sep_cma_es(prob, z0, 0.3, 64, prob.sampled_plain, 10, seed=11,
+                                      generations=a.fit_gens)
+    runs["es_batched"] = fit.sep_cma_es(prob, z0, 0.3, 64, prob.sampled_batched, 10, seed=11,
+                                        generations=a.fit_gens)
+    runs["adam"] = fit.adam(prob, z0, steps=a.fit_steps, lr=0.05, samples=16, seed=5)
+    clocks.mark()
+    time.sleep(0.2)
+    clocks.stop()
+    curves = {k: [yard(z) for z in r.best_z] for k, r in runs.items()}
+    y_true, y0 = yard(z_true), yard(z0)
+    target = curves["es_plain"][-1]
+
+    def ttf(k):
+        for t, y in zip(runs[k].times, curves[k]):
+            if y <= target:
+                return t
+        return None
+
+    out = {}
+    for k, r in runs.items():
+        out[k] = {"time_to_target_s": ttf(k), "total_s": r.times[-1], "iterations": len(r.times),
+                  "param_sets_evaluated": r.evals, "final_chi2": curves[k][-1],
+                  "best_chi2": min(curves[k])}
+    base = out["es_plain"]["time_to_target_s"]
+    adam_t = out["adam"]["time_to_target_s"]
+    line = {"metric": "time-to-fit at fixed chi-square", "value": adam_t, "unit": "s",
+            "n_gpus": 1, "steps": a.fit_steps, "warmup": 1, "ms_per_step": 1e3 * out["adam"]["total_s"] / out["adam"]["iterations"],
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 masses / f64 chi-square", "data": "synthetic (seeded)",
+            "config": {"workload": "fit_4state", "bursts": bs.B, "states": n, "free_rates": int(prob.free.size),
+                       "nbins": md["nbins"],
+                       "es_population": 64, "es_samples": 10, "es_generations": a.fit_gens,
+                       "adam_samples": 16, "adam_lr": 0.05, "yardstick": "expected chi2, 32 samples, seed 0x5EED"},
+            "target_chi2": target, "chi2_true": y_true, "chi2_start": y0,
+            "speedup_vs_es_plain": (base / adam_t) if (base and adam_t) else None,
+            "runs": out, "clocks": clocks.summary(),
+            "fitted_E": [float(x) for x in prob.to_args(runs["adam"].z)[0][:n]]}
+    print(json.dumps(line), flush=True)
+    eng.close()
+    return 0
+
+
 def main():
     a = parse()
+    if a.workload == "fit_4state":
+        return run_fit(a)
     if a.impl == "reference":
         return run_reference(a)
     if a.workload == "population_256":
