@@ -239,16 +239,28 @@ def run_population(a):
     ohist, _ = eng.run_plain(MODE_OCCUPANCY, n, args[0], 1, HELD_OUT_SEED)
     eng.set_observed(ohist.astype(np.float32))
     units = P * bs.B * S
+    # launch-based batched step (one asynchronous launch per step)
     for w in range(a.warmup):
         eng.launch(MODE_OCCUPANCY, n, args, S, 100 + w)
     eng.synchronize()
     t0 = time.perf_counter()
-    kms = []
     for k in range(a.steps):
         eng.launch(MODE_OCCUPANCY, n, args, S, 200 + k)
+    eng.fetch(P)
+    launch_s = (time.perf_counter() - t0) / a.steps
+    # autotuned tile, then the whole step captured as one CUDA graph
+    tile = eng.autotune(MODE_OCCUPANCY, n, args, S)
+    eng.graph_create(MODE_OCCUPANCY, n, P, S)
+    for w in range(a.warmup):
+        eng.graph_run(args, 100 + w)
+    l0 = eng.launch_count
+    t0 = time.perf_counter()
+    kms = []
+    for k in range(a.steps):
+        hist, chi2 = eng.graph_run(args, 200 + k)
         kms.append(eng.lib.gpda_kernel_ms(eng.ctx))
-    hist, chi2 = eng.fetch(P)
     batched_s = (time.perf_counter() - t0) / a.steps
+    launches = eng.launch_count - l0
     # plain: one launch + fetch per parameter set
     eng.run_plain(MODE_OCCUPANCY, n, args[0], S, 1)
     t0 = time.perf_counter()
@@ -270,8 +282,10 @@ def run_population(a):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded)",
             "config": {"workload": "population_256", "bursts": bs.B, "samples": S, "states": n,
-                       "param_sets": P, "mode": "occupancy"},
+                       "param_sets": P, "mode": "occupancy", "graph": True, "tile_bursts": tile},
+            "gpu_launches": int(launches),
             "kernel_ms": sum(kms) / len(kms),
+            "launch_value": units / launch_s,
             "plain_value": units / plain_s,
             "batched_over_plain": plain_s / batched_s,
             "refflow_value": units / refflow_s,

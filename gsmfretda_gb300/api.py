@@ -120,6 +120,30 @@ class Engine:
                                        _p(units), _p(hist)), self.ctx)
         return units, hist
 
+    # ---------------------------------------------------------------- captured launch
+    def graph_create(self, mode, n, P, samples):
+        """Capture one batched step (P parameter sets) as a CUDA graph."""
+        _check(self.lib.gpda_graph_create(self.ctx, mode, P, n, samples), self.ctx)
+        self._graph = (n, P)
+
+    def graph_run(self, args, seed):
+        n, P = self._graph
+        a = np.ascontiguousarray(args, dtype=np.float32).reshape(-1)
+        if a.size != P * n * (n + 1):
+            raise ValueError("args must hold the captured number of parameter sets")
+        hist = np.zeros((P, self.nbins), dtype=np.uint64)
+        chi2 = np.zeros(P, dtype=np.float64)
+        _check(self.lib.gpda_graph_run(self.ctx, _p(a), seed, _p(hist), _p(chi2)), self.ctx)
+        return hist, chi2
+
+    def autotune(self, mode, n, args, samples, seed=1):
+        """Pick the fastest bursts-per-work-item for this launch shape; returns it."""
+        a = np.ascontiguousarray(args, dtype=np.float32).reshape(-1)
+        P = a.size // (n * (n + 1))
+        t = C.c_int32(0)
+        _check(self.lib.gpda_autotune(self.ctx, mode, P, n, _p(a), samples, seed, C.byref(t)), self.ctx)
+        return t.value
+
     # ---------------------------------------------------------------- expected histogram
     def _exp_args(self, n, args, anchor):
         a = np.ascontiguousarray(args, dtype=np.float32).reshape(-1)

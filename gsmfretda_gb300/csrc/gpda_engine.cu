@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -76,6 +77,17 @@ struct gpda_ctx {
     bool exp_valid = false;         // the forward state matches exp_key
     std::vector<float> exp_key;
     int exp_P = 0, exp_nblk = 0;
+    // autotuned bursts per work item: {mode, samples, tile}
+    std::vector<std::array<int, 3>> tuned;
+    // captured batched launch (gpda_graph_create / gpda_graph_run)
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    cudaGraphNode_t gnode = nullptr;     // the Monte-Carlo kernel node
+    cudaKernelNodeParams gkp{};
+    PdaArgs gargs{};
+    void *gargv[1] = {nullptr};
+    int g_mode = 0, g_P = 0, g_n = 0, g_S = 0, g_kernels = 0;
+    bool g_chi2 = false;
     // last launch
     int last_P = 0;
     bool last_chi2 = false;
@@ -120,8 +132,11 @@ int check_model(const gpda_model *m) {
     return 0;
 }
 
+void free_graph(gpda_ctx *c);
+
 int ensure_scratch(gpda_ctx *c, int P) {
     int nb = c->model.nbins;
+    if (P > c->cap_P || P * nb > c->cap_hist) free_graph(c);   // the graph holds these buffers
     if (P > c->cap_P) {
         free_dev(c->dParams);
         if (c->hParams) cudaFreeHost(c->hParams);
@@ -149,12 +164,23 @@ int ensure_scratch(gpda_ctx *c, int P) {
 }
 
 int tile_bursts(const gpda_ctx *c, int mode, int S) {
+    for (const auto &t : c->tuned)
+        if (t[0] == mode && t[1] == S) return t[2];
     int tb = (2048 + S - 1) / S;
     if (mode == GPDA_MODE_PHOTON && c->mean_N > 0.0) {
         int fit = (int)(0.6 * kSmemCapFloats / c->mean_N);
         tb = std::min(tb, std::max(fit, 1));
     }
     return std::max(1, std::min(tb, kMaxTileBursts));
+}
+
+void free_graph(gpda_ctx *c) {
+    if (c->gexec) cudaGraphExecDestroy(c->gexec);
+    if (c->graph) cudaGraphDestroy(c->graph);
+    c->gexec = nullptr;
+    c->graph = nullptr;
+    c->gnode = nullptr;
+    c->g_P = 0;
 }
 
 int do_launch(gpda_ctx *c, int mode, int P, int n, const float *params, int64_t b0, int64_t b1,
@@ -183,6 +209,7 @@ int do_launch(gpda_ctx *c, int mode, int P, int n, const float *params, int64_t 
         const size_t ntab = (size_t)P * n;
         if (ntab > c->cap_tab) {
             CK(cudaStreamSynchronize(c->stream));
+            free_graph(c);
             free_dev(c->dCdf);
             free_dev(c->dGuide);
             c->dCdf = nullptr; c->dGuide = nullptr; c->cap_tab = 0;
@@ -469,6 +496,7 @@ void gpda_destroy(gpda_ctx *c) {
     free_dev(c->dObs); free_dev(c->dParams); free_dev(c->dHist); free_dev(c->dChi2);
     free_dev(c->dWork); free_dev(c->dLimit); free_dev(c->dUnit); free_dev(c->dFlag);
     free_dev(c->dCdf); free_dev(c->dGuide);
+    free_graph(c);
     free_dev(c->dExp); free_dev(c->dExpPart); free_dev(c->dExpGPart); free_dev(c->dExpHist);
     free_dev(c->dExpChi2); free_dev(c->dExpGrad); free_dev(c->dExpUp); free_dev(c->dExpG);
     free_dev(c->dExpInv);
@@ -501,6 +529,7 @@ int32_t gpda_upload_bursts(gpda_ctx *c, const int32_t *N, const float *T, const 
     CK(cudaStreamSynchronize(c->stream));
     c->B = 0;
     c->exp_valid = false;
+    free_graph(c);
     // grow-only device store; contents are validated on the device below
     if (B > c->cap_B) {
         free_dev(c->dN); free_dev(c->dT); free_dev(c->dOffIdx);
@@ -550,8 +579,12 @@ int32_t gpda_upload_bursts(gpda_ctx *c, const int32_t *N, const float *T, const 
 }
 
 int32_t gpda_set_observed(gpda_ctx *c, const float *ohist, int32_t nbins) {
-    if (c) c->exp_valid = false;
     if (!c) return GPDA_ERR_ARG;
+    c->exp_valid = false;
+    if (!c->has_obs) {
+        cudaStreamSynchronize(c->stream);
+        free_graph(c);          // a graph captured without the chi-square node
+    }
     if (!ohist || nbins != c->model.nbins) return fail(c, GPDA_ERR_ARG, "observed histogram must have model.nbins bins");
     CK(cudaSetDevice(c->device));
     CK(cudaMemcpyAsync(c->dObs, ohist, sizeof(float) * nbins, cudaMemcpyHostToDevice, c->stream));
@@ -703,6 +736,156 @@ int32_t gpda_expected_grad(gpda_ctx *c, int32_t P, int32_t n, const float *param
     if (!c) return GPDA_ERR_ARG;
     if (!chi2_out) return fail(c, GPDA_ERR_ARG, "chi2_out");
     return exp_run(c, P, n, params, anchor, S, seed, hist_out, chi2_out, true, nullptr, dE, dlogK);
+}
+
+int32_t gpda_graph_create(gpda_ctx *c, int32_t mode, int32_t P, int32_t n, int32_t S) {
+    if (!c) return GPDA_ERR_ARG;
+    if (mode != GPDA_MODE_OCCUPANCY && mode != GPDA_MODE_PHOTON) return fail(c, GPDA_ERR_ARG, "mode");
+    if (P < 1 || n < 1 || n > GPDA_MAX_STATES || S < 1) return fail(c, GPDA_ERR_ARG, "P, n_states or samples");
+    if (c->B == 0 || !c->dN) return fail(c, GPDA_ERR_STATE, "no bursts uploaded");
+    if (mode == GPDA_MODE_PHOTON && !c->has_offsets) return fail(c, GPDA_ERR_STATE, "photon mode needs arrival offsets");
+    if (c->B * (int64_t)S > (int64_t)INT32_MAX) return fail(c, GPDA_ERR_ARG, "too many units per parameter set");
+    CK(cudaSetDevice(c->device));
+    CK(cudaStreamSynchronize(c->stream));
+    free_graph(c);
+    int rc = ensure_scratch(c, P);
+    if (rc) return rc;
+    if (mode == GPDA_MODE_PHOTON && (size_t)P * n > c->cap_tab) {
+        free_dev(c->dCdf);
+        free_dev(c->dGuide);
+        c->dCdf = nullptr; c->dGuide = nullptr; c->cap_tab = 0;
+        CK(cudaMalloc(&c->dCdf, sizeof(float) * kTableRows * (size_t)P * n));
+        CK(cudaMalloc(&c->dGuide, sizeof(uint16_t) * kTableRows * (size_t)P * n));
+        c->cap_tab = (size_t)P * n;
+    }
+    const int nbins = c->model.nbins;
+    PdaArgs a{};
+    a.bcdf = c->dCdf; a.bguide = c->dGuide;
+    a.N = c->dN; a.T = c->dT; a.off_idx = c->dOffIdx; a.offsets = c->dOff;
+    a.params = c->dParams; a.hist = c->dHist; a.unit_out = nullptr; a.work = c->dWork;
+    a.limit_hits = c->dLimit;
+    a.b0 = 0; a.b1 = c->B; a.seed = 0; a.P = P; a.S = S;
+    a.tile_b = tile_bursts(c, mode, S);
+    int64_t ntiles = (c->B + a.tile_b - 1) / a.tile_b;
+    if (ntiles * P > (int64_t)INT32_MAX) return fail(c, GPDA_ERR_ARG, "too many work items");
+    a.ntiles = (int)ntiles; a.n_items = (int)(ntiles * P); a.nbins = nbins;
+    a.smem_cap = kSmemCapFloats; a.pbase = 0u;
+    a.gamma = c->model.gamma; a.ct = c->model.crosstalk; a.r0 = c->model.r0;
+    a.bg_a = c->model.bg_a; a.bg_d = c->model.bg_d;
+    const size_t dyn = (mode == GPDA_MODE_PHOTON) ? sizeof(float) * kSmemCapFloats : 0;
+    const int grid = (int)std::min<int64_t>(a.n_items, (int64_t)c->num_sms * c->blocks_per_sm[mode]);
+    // one stream capture of the whole batched step
+    CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    int kernels = 0;
+    cudaError_t e = cudaMemcpyAsync(c->dParams, c->hParams, sizeof(DevParams) * P, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess && mode == GPDA_MODE_PHOTON) { e = launch_binom_tables(c->dParams, P, n, c->dCdf, c->dGuide, c->stream); kernels++; }
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->dHist, 0, sizeof(unsigned long long) * (size_t)P * nbins, c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->dWork, 0, sizeof(unsigned int), c->stream);
+    if (e == cudaSuccess) { e = launch_pda(mode, a, grid, dyn, c->stream); kernels++; }
+    if (e == cudaSuccess && c->has_obs) { e = launch_chi2(c->dHist, c->dObs, P, nbins, c->model.left_pad, S, n, c->dChi2, c->stream); kernels++; }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(c->hHist, c->dHist, sizeof(unsigned long long) * (size_t)P * nbins, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess && c->has_obs) e = cudaMemcpyAsync(c->hChi2, c->dChi2, sizeof(double) * P, cudaMemcpyDeviceToHost, c->stream);
+    cudaGraph_t g = nullptr;
+    cudaError_t e2 = cudaStreamEndCapture(c->stream, &g);
+    if (e != cudaSuccess || e2 != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        cudaGetLastError();
+        return cuda_fail(c, e != cudaSuccess ? e : e2, "graph capture");
+    }
+    c->graph = g;
+    // the Monte-Carlo kernel node, whose seed each replay sets
+    size_t nn = 0;
+    CK(cudaGraphGetNodes(g, nullptr, &nn));
+    std::vector<cudaGraphNode_t> nodes(nn);
+    CK(cudaGraphGetNodes(g, nodes.data(), &nn));
+    for (auto nd : nodes) {
+        cudaGraphNodeType t;
+        CK(cudaGraphNodeGetType(nd, &t));
+        if (t != cudaGraphNodeTypeKernel) continue;
+        cudaKernelNodeParams kp{};
+        CK(cudaGraphKernelNodeGetParams(nd, &kp));
+        if (kp.func == pda_kernel_fn(mode)) {
+            c->gnode = nd;
+            c->gkp = kp;
+        }
+    }
+    if (!c->gnode) { free_graph(c); return fail(c, GPDA_ERR_STATE, "graph capture: kernel node not found"); }
+    CK(cudaGraphInstantiate(&c->gexec, g, 0));
+    c->gargs = a;
+    c->gargv[0] = &c->gargs;
+    c->gkp.kernelParams = c->gargv;
+    c->gkp.extra = nullptr;
+    c->g_mode = mode; c->g_P = P; c->g_n = n; c->g_S = S; c->g_kernels = kernels;
+    c->g_chi2 = c->has_obs;
+    return GPDA_OK;
+}
+
+int32_t gpda_graph_run(gpda_ctx *c, const float *params, uint64_t seed, uint64_t *hist_out,
+                       double *chi2_out) {
+    if (!c) return GPDA_ERR_ARG;
+    if (!c->gexec) return fail(c, GPDA_ERR_STATE, "no captured launch (gpda_graph_create first)");
+    if (!params) return fail(c, GPDA_ERR_ARG, "params");
+    CK(cudaSetDevice(c->device));
+    CK(cudaStreamSynchronize(c->stream));    // pinned staging is free
+    const int P = c->g_P, n = c->g_n, nb = c->model.nbins;
+    const size_t stride = (size_t)n * (n + 1);
+    for (int p = 0; p < P; ++p) {
+        int r = build_params(n, params + stride * p, c->model.gamma, c->model.crosstalk, true, &c->hParams[p]);
+        if (r == -2) return fail(c, GPDA_ERR_SINGULAR, "rate matrix has no unique stationary distribution (parameter set " + std::to_string(p) + ")");
+        if (r != 0) return fail(c, GPDA_ERR_ARG, "invalid parameter vector " + std::to_string(p));
+    }
+    c->gargs.seed = seed;
+    CK(cudaGraphExecKernelNodeSetParams(c->gexec, c->gnode, &c->gkp));
+    CK(cudaEventRecord(c->k0, c->stream));
+    CK(cudaGraphLaunch(c->gexec, c->stream));
+    CK(cudaEventRecord(c->k1, c->stream));
+    c->timed = true;
+    c->launches += c->g_kernels;
+    c->last_P = P;
+    c->last_chi2 = c->g_chi2;
+    CK(cudaStreamSynchronize(c->stream));
+    if (hist_out) std::memcpy(hist_out, c->hHist, sizeof(uint64_t) * (size_t)P * nb);
+    if (chi2_out) {
+        if (c->g_chi2) std::memcpy(chi2_out, c->hChi2, sizeof(double) * P);
+        else for (int p = 0; p < P; ++p) chi2_out[p] = NAN;
+    }
+    return GPDA_OK;
+}
+
+int32_t gpda_autotune(gpda_ctx *c, int32_t mode, int32_t P, int32_t n, const float *params,
+                      int32_t S, uint64_t seed, int32_t *tile_out) {
+    if (!c) return GPDA_ERR_ARG;
+    if (mode != GPDA_MODE_OCCUPANCY && mode != GPDA_MODE_PHOTON) return fail(c, GPDA_ERR_ARG, "mode");
+    CK(cudaSetDevice(c->device));
+    // forget an earlier choice for this shape, then time candidates around the default
+    for (size_t i = 0; i < c->tuned.size(); ++i)
+        if (c->tuned[i][0] == mode && c->tuned[i][1] == S) { c->tuned.erase(c->tuned.begin() + i); break; }
+    const int base = tile_bursts(c, mode, S);
+    std::vector<int> cand;
+    for (int f : {-2, -1, 0, 1, 2}) {
+        int t = f < 0 ? base >> (-f) : base << f;
+        t = std::max(1, std::min(t, kMaxTileBursts));
+        if (std::find(cand.begin(), cand.end(), t) == cand.end()) cand.push_back(t);
+    }
+    int best = base;
+    float best_ms = 1e30f;
+    for (int t : cand) {
+        c->tuned.push_back({mode, S, t});
+        float ms = 0.0f;
+        for (int r = 0; r < 3; ++r) {
+            int rc = do_launch(c, mode, P, n, params, 0, c->B, S, seed + (uint64_t)r, nullptr);
+            if (rc) { c->tuned.pop_back(); return rc; }
+            float k = gpda_kernel_ms(c);
+            if (r > 0) ms += k;      // the first launch warms the caches
+        }
+        c->tuned.pop_back();
+        if (ms < best_ms) { best_ms = ms; best = t; }
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    free_graph(c);               // a captured launch uses the old tile
+    c->tuned.push_back({mode, S, best});
+    if (tile_out) *tile_out = best;
+    return GPDA_OK;
 }
 
 }  // extern "C"

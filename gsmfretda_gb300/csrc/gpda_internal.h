@@ -95,6 +95,7 @@ struct RcArgs {
 
 // kernel launchers (gpda_kernels.cu)
 cudaError_t launch_pda(int mode, const PdaArgs &a, int grid, size_t dyn_smem, cudaStream_t st);
+const void *pda_kernel_fn(int mode);   // the kernel launch_pda(mode) runs
 cudaError_t launch_chi2(const unsigned long long *hist, const float *obs, int P, int nbins,
                         int left_pad, int S, int n_states, double *chi2, cudaStream_t st);
 cudaError_t launch_rc(const RcArgs &a, cudaStream_t st);

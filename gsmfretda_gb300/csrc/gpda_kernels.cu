@@ -606,6 +606,11 @@ cudaError_t launch_validate(const int32_t *N, const float *T, const int64_t *off
     return cudaGetLastError();
 }
 
+const void *pda_kernel_fn(int mode) {
+    return mode == 0 ? reinterpret_cast<const void *>(&pda_kernel<0>)
+                     : reinterpret_cast<const void *>(&pda_kernel<1>);
+}
+
 cudaError_t launch_pda(int mode, const PdaArgs &a, int grid, size_t dyn_smem, cudaStream_t st) {
     if (mode == 0) pda_kernel<0><<<grid, kThreads, dyn_smem, st>>>(a);
     else pda_kernel<1><<<grid, kThreads, dyn_smem, st>>>(a);

@@ -151,6 +151,29 @@ float gpda_kernel_ms(gpda_ctx *ctx);
 /* Number of units whose segment/rejection loops hit their bound so far. */
 int64_t gpda_limit_hits(gpda_ctx *ctx);
 
+/* ---- Captured batched launch and tile autotuning (no counterpart in the
+ * reference, which launches one kernel per parameter set).
+ *
+ * gpda_graph_create captures one batched step over all uploaded bursts for
+ * (mode, P, n_states, samples) as a CUDA graph: parameter copy, binomial
+ * tables (photon mode), histogram reset, the Monte-Carlo kernel, the
+ * chi-square (when an observed histogram is set) and the read-back into the
+ * context's pinned buffers. gpda_graph_run replays it for P parameter vectors
+ * and a seed, with results identical to gpda_run_batched with the same
+ * arguments. Uploading bursts, setting the first observed histogram, a
+ * larger launch on the context or gpda_autotune drop the graph (then
+ * gpda_graph_run returns GPDA_ERR_STATE). */
+int32_t gpda_graph_create(gpda_ctx *ctx, int32_t mode, int32_t P, int32_t n_states,
+                          int32_t samples);
+int32_t gpda_graph_run(gpda_ctx *ctx, const float *params, uint64_t seed, uint64_t *hist_out,
+                       double *chi2_out);
+/* Times the Monte-Carlo kernel for bursts per work item around the default
+ * for (mode, samples) on these parameter vectors and keeps the fastest for
+ * later launches of that shape on this context (tile_out, nullable). The
+ * tile does not change any result. */
+int32_t gpda_autotune(gpda_ctx *ctx, int32_t mode, int32_t P, int32_t n_states,
+                      const float *params, int32_t samples, uint64_t seed, int32_t *tile_out);
+
 /* ---- Differentiable expected histogram (occupancy model), no counterpart
  * in the reference: the gradient path of the parameter-server side.
  *

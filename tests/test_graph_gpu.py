@@ -1,0 +1,66 @@
+"""Captured batched launches (gpda_graph_create / gpda_graph_run) and tile
+autotuning: replays equal gpda_run_batched bit for bit whatever the seed and
+parameters of each replay, the tile chosen by the autotuner changes no result,
+and uploading bursts drops the captured graph."""
+import numpy as np
+import pytest
+
+from gsmfretda_gb300 import synth
+from gsmfretda_gb300._lib import GpdaError
+from gsmfretda_gb300.api import MODE_OCCUPANCY, MODE_PHOTON, Engine
+
+pytestmark = pytest.mark.gpu
+
+
+def _population(P, seed):
+    return synth.population_args(P, seed)
+
+
+def test_graph_replays_match_batched_occupancy(gpda_lib):
+    bs, n, _, md, S = synth.population_256(B=3000, P=8, seed=31)
+    with Engine(0, **md) as eng:
+        eng.upload(bs)
+        ref_h, _ = eng.run_plain(MODE_OCCUPANCY, n, _population(1, 1)[0], 1, 5)
+        eng.set_observed(ref_h.astype(np.float32))
+        eng.graph_create(MODE_OCCUPANCY, n, 8, S)
+        for r in range(3):
+            args = _population(8, 100 + r)
+            hg, cg = eng.graph_run(args, 1000 + r)
+            hb, cb = eng.run_batched(MODE_OCCUPANCY, n, args, S, 1000 + r)
+            np.testing.assert_array_equal(hg, hb)
+            np.testing.assert_array_equal(cg, cb)
+        # a different seed changes the result
+        h2, _ = eng.graph_run(_population(8, 100), 5555)
+        assert not np.array_equal(h2, eng.run_batched(MODE_OCCUPANCY, n, _population(8, 100), S, 1000)[0])
+
+
+def test_graph_replays_match_batched_photon(gpda_lib):
+    bs, n, args, md, S = synth.photon_3state(B=1500, seed=32)
+    rng = np.random.default_rng(3)
+    with Engine(0, **md) as eng:
+        eng.upload(bs)
+        eng.graph_create(MODE_PHOTON, n, 2, 20)
+        for r in range(2):
+            a2 = np.stack([synth.random_3state_args(rng) for _ in range(2)])
+            hg, cg = eng.graph_run(a2, 77 + r)
+            hb, cb = eng.run_batched(MODE_PHOTON, n, a2, 20, 77 + r)
+            np.testing.assert_array_equal(hg, hb)
+            assert np.all(np.isnan(cg))          # no observed histogram: no chi-square
+
+
+def test_autotune_changes_no_result_and_upload_drops_the_graph(gpda_lib):
+    bs, n, _, md, S = synth.population_256(B=4000, P=4, seed=33)
+    args = _population(4, 9)
+    with Engine(0, **md) as eng:
+        eng.upload(bs)
+        h0, _ = eng.run_batched(MODE_OCCUPANCY, n, args, S, 42)
+        tile = eng.autotune(MODE_OCCUPANCY, n, args, S)
+        assert 1 <= tile <= 256
+        h1, _ = eng.run_batched(MODE_OCCUPANCY, n, args, S, 42)
+        np.testing.assert_array_equal(h0, h1)
+        eng.graph_create(MODE_OCCUPANCY, n, 4, S)
+        hg, _ = eng.graph_run(args, 42)
+        np.testing.assert_array_equal(hg, h0)
+        eng.upload(bs)
+        with pytest.raises(GpdaError):
+            eng.graph_run(args, 42)
