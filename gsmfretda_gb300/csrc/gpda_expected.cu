@@ -351,42 +351,60 @@ __global__ void __launch_bounds__(kExpThreads) exp_fwd_kernel(const ExpArgs a) {
     }
 }
 
-// One block per parameter set, one thread per bin.
-__global__ void exp_chi2_kernel(const ExpArgs a) {
+// sum over k < count of src[k * stride] in a fixed order: lane l adds
+// k = l, l + 32, ... in turn, then a fixed shuffle tree; the result is in lane 0
+__device__ __forceinline__ double warp_sum_strided(const double *src, int count, size_t stride,
+                                                   int lane) {
+    double v = 0.0;
+    for (int k = lane; k < count; k += 32) v += src[(size_t)k * stride];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// One block of 256 threads per parameter set: a warp per bin sums the
+// per-block partials, then the chi-square (sequential over bins, FP64, as
+// chi2_kernel) and d chi2 / d count for each bin.
+__global__ void __launch_bounds__(256) exp_chi2_kernel(const ExpArgs a) {
     __shared__ double sM[kExpMaxBins];
+    __shared__ double s_den;
     const int p = blockIdx.x;
-    const int bin = threadIdx.x;
-    if (bin < a.nbins) {
-        const double *src = a.part + (size_t)p * a.nblk * a.nbins + bin;
-        double v = 0.0;
-        for (int k = 0; k < a.nblk; ++k) v += src[(size_t)k * a.nbins];
-        sM[bin] = v;
-        a.hist[(size_t)p * a.nbins + bin] = v;
-    }
-    __syncthreads();
-    if (bin != 0) return;
-    int effN = a.nbins - a.left_pad;
-    double chi = 0.0;
-    for (int i = a.left_pad; i < a.nbins; ++i) {
-        if (sM[i] > 0.0) {
-            double mi = sM[i] / (double)a.S;
-            double d = (double)a.obs[i] - mi;
-            chi = chi + d * d / mi;
-        } else {
-            effN -= 1;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int bin = warp; bin < a.nbins; bin += 8) {
+        double v = warp_sum_strided(a.part + (size_t)p * a.nblk * a.nbins + bin, a.nblk,
+                                    (size_t)a.nbins, lane);
+        if (lane == 0) {
+            sM[bin] = v;
+            a.hist[(size_t)p * a.nbins + bin] = v;
         }
     }
-    const double den = (double)(effN - a.n * (a.n + 1));
-    a.chi2[p] = chi / den;
-    float *g = a.g + (size_t)p * a.nbins;
-    for (int i = 0; i < a.nbins; ++i) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int effN = a.nbins - a.left_pad;
+        double chi = 0.0;
+        for (int i = a.left_pad; i < a.nbins; ++i) {
+            if (sM[i] > 0.0) {
+                double mi = sM[i] / (double)a.S;
+                double d = (double)a.obs[i] - mi;
+                chi = chi + d * d / mi;
+            } else {
+                effN -= 1;
+            }
+        }
+        const double den = (double)(effN - a.n * (a.n + 1));
+        a.chi2[p] = chi / den;
+        s_den = den;
+    }
+    __syncthreads();
+    const int i = threadIdx.x;
+    if (i < a.nbins) {
         double gi = 0.0;
         if (i >= a.left_pad && sM[i] > 0.0) {
             double mi = sM[i] / (double)a.S;
             double o = (double)a.obs[i];
-            gi = (1.0 - (o * o) / (mi * mi)) / ((double)a.S * den);
+            gi = (1.0 - (o * o) / (mi * mi)) / ((double)a.S * s_den);
         }
-        g[i] = (float)gi;
+        a.g[(size_t)p * a.nbins + i] = (float)gi;
     }
 }
 
@@ -473,16 +491,20 @@ __global__ void __launch_bounds__(kExpThreads) exp_adj_kernel(const ExpArgs a) {
     }
 }
 
-__global__ void exp_grad_kernel(const ExpArgs a) {
+// One block of kExpGrad warps per parameter set: warp k sums component k of
+// the per-block partials in a fixed order and scales it by the upstream
+// gradient.
+__global__ void __launch_bounds__(32 * kExpGrad) exp_grad_kernel(const ExpArgs a) {
     const int p = blockIdx.x;
-    const int k = threadIdx.x;
+    const int k = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int ng = a.n + a.n * (a.n - 1);
     if (k >= ng) return;
-    const double *src = a.gpart + (size_t)p * a.nblk_adj * kExpGrad + k;
-    double v = 0.0;
-    for (int j = 0; j < a.nblk_adj; ++j) v += src[(size_t)j * kExpGrad];
-    const double up = a.dchi2 ? a.dchi2[p] : 1.0;
-    a.grad[(size_t)p * kExpGrad + k] = v * up;
+    double v = warp_sum_strided(a.gpart + (size_t)p * a.nblk_adj * kExpGrad + k, a.nblk_adj,
+                                (size_t)kExpGrad, lane);
+    if (lane == 0) {
+        const double up = a.dchi2 ? a.dchi2[p] : 1.0;
+        a.grad[(size_t)p * kExpGrad + k] = v * up;
+    }
 }
 
 __global__ void inv_table_kernel(float *inv) {
@@ -527,7 +549,7 @@ cudaError_t launch_exp_forward(const ExpArgs &a, cudaStream_t st) {
     default: return cudaErrorInvalidValue;
     }
     if (e != cudaSuccess) return e;
-    exp_chi2_kernel<<<a.P, kExpMaxBins, 0, st>>>(a);
+    exp_chi2_kernel<<<a.P, 256, 0, st>>>(a);
     return cudaGetLastError();
 }
 
@@ -541,7 +563,7 @@ cudaError_t launch_exp_adjoint(const ExpArgs &a, cudaStream_t st) {
     default: return cudaErrorInvalidValue;
     }
     if (e != cudaSuccess) return e;
-    exp_grad_kernel<<<a.P, 32, 0, st>>>(a);
+    exp_grad_kernel<<<a.P, 32 * kExpGrad, 0, st>>>(a);
     return cudaGetLastError();
 }
 
