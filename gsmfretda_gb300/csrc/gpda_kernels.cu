@@ -135,36 +135,39 @@ __device__ __forceinline__ bool step_pho(Unit &U, const DevParams &P, const floa
     return false;
 }
 
-// Occupancy mode: one dwell segment per step, draws [state, dwell]; after the
-// last one, a fresh block for the background and the single binomial split
-// with the occupancy-weighted efficiency.
-__device__ __forceinline__ bool step_occ(Unit &U, const DevParams &P, float g, float ct, float r0,
-                                         float bga, float bgd, int &lim, const float *inv) {
+// Occupancy mode: one dwell segment per step, draws [state, dwell]; returns
+// true once the trajectory has reached the end of the burst (U.acc then holds
+// the occupancy-weighted efficiency times T). The background and binomial
+// split follow in final_occ.
+__device__ __forceinline__ bool traj_occ(Unit &U, const DevParams &P, float r0, int &lim) {
     const int st = next_state(U, P, U.r.u01());
     U.st = st;
-    if (U.Tb > 0.0f) {
-        float u = U.r.u01();
-        float tau = (P.kexit[st] > 0.0f) ? (-logf_(u)) * P.inv_kexit[st] : kInf;
-        float tn = U.t + tau;
-        bool cut = U.seg == kMaxSeg - 1;
-        bool last = !(tn < U.Tb) || cut;
-        if (cut && tn < U.Tb) lim += 1;
-        float dt = last ? U.Tb - U.t : tn - U.t;
-        float es = P.E[st];
-        if (P.V[st] > 0.0f) es = broaden(U.r, es, r0, P.V[st]);
-        U.acc = fmaf(dt, es, U.acc);
-        if (!last) {
-            U.t = tn;
-            U.seg += 1;
-            return false;
-        }
-    }
-    float eeff = (U.Tb > 0.0f) ? U.acc / U.Tb : P.E[st];
+    if (!(U.Tb > 0.0f)) return true;
+    float u = U.r.u01();
+    float tau = (P.kexit[st] > 0.0f) ? (-logf_(u)) * P.inv_kexit[st] : kInf;
+    float tn = U.t + tau;
+    bool cut = U.seg == kMaxSeg - 1;
+    bool last = !(tn < U.Tb) || cut;
+    if (cut && tn < U.Tb) lim += 1;
+    float dt = last ? U.Tb - U.t : tn - U.t;
+    float es = P.E[st];
+    if (P.V[st] > 0.0f) es = broaden(U.r, es, r0, P.V[st]);
+    U.acc = fmaf(dt, es, U.acc);
+    if (last) return true;
+    U.t = tn;
+    U.seg += 1;
+    return false;
+}
+
+// Occupancy mode, after the trajectory: a fresh block for the background and
+// the single binomial split with the occupancy-weighted efficiency.
+__device__ __forceinline__ void final_occ(Unit &U, const DevParams &P, float g, float ct, float bga,
+                                          float bgd, int &lim, const float *inv) {
+    float eeff = (U.Tb > 0.0f) ? U.acc / U.Tb : P.E[U.st];
     U.r.align();
     int sig;
     int ba = background(U.r, U.Nb, bga * U.Tb, bgd * U.Tb, &sig, lim, inv);
     U.A = binom(U.r, sig, eps_of(eeff, g, ct), lim, inv) + ba;
-    return true;
 }
 
 // warp-aggregated shared-memory histogram increment; all 32 lanes call it
@@ -245,22 +248,38 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) pda_kernel(const PdaArgs
         const uint32_t pw = a.pbase + (uint32_t)p;
         Unit U;
         bool active = tid < units;
+        bool ready = false;     // occupancy mode: trajectory done, split pending
         if (active) unit_begin(U, tid, a.S, tb0, sN, sT, a.seed, pw);
         while (__any_sync(0xffffffffu, active)) {
             bool fin = false;
             int bin = -1;
-            if (active) {
+            if (MODE == 0) {
+                // Trajectory steps are cheap and the background + binomial
+                // split is not: lanes whose trajectory has ended wait, and the
+                // warp runs their splits together once enough are waiting (or
+                // nothing else is left), instead of a few lanes at a time.
+                if (active && !ready) {
+                    if (U.done) fin = true;
+                    else ready = traj_occ(U, sp, a.r0, lim);
+                }
+                const unsigned rmask = __ballot_sync(0xffffffffu, active && ready);
+                const unsigned tmask = __ballot_sync(0xffffffffu, active && !ready && !fin);
+                if (rmask && (__popc(rmask) >= GPDA_FIN_MIN || tmask == 0) && ready) {
+                    final_occ(U, sp, a.gamma, a.ct, a.bg_a, a.bg_d, lim, s_inv);
+                    ready = false;
+                    fin = true;
+                }
+            }
+            if (MODE == 1 && active) {
                 fin = U.done;
                 if (!fin) {
-                    if (MODE == 0) {
-                        fin = step_occ(U, sp, a.gamma, a.ct, a.r0, a.bg_a, a.bg_d, lim, s_inv);
-                    } else {
-                        const float *offs = staged ? (s_ph + sOff[U.lb]) : (a.offsets + a.off_idx[tb0 + U.lb]);
-                        fin = step_pho(U, sp, offs, a.gamma, a.ct, a.r0, a.bg_a, a.bg_d, lim, s_inv,
-                                       a.bcdf + (size_t)p * sp.n * kTableRows,
-                                       a.bguide + (size_t)p * sp.n * kTableRows);
-                    }
+                    const float *offs = staged ? (s_ph + sOff[U.lb]) : (a.offsets + a.off_idx[tb0 + U.lb]);
+                    fin = step_pho(U, sp, offs, a.gamma, a.ct, a.r0, a.bg_a, a.bg_d, lim, s_inv,
+                                   a.bcdf + (size_t)p * sp.n * kTableRows,
+                                   a.bguide + (size_t)p * sp.n * kTableRows);
                 }
+            }
+            if (active) {
                 if (fin) {
                     const int64_t b = tb0 + U.lb;
                     if (a.unit_out) a.unit_out[((int64_t)p * (a.b1 - a.b0) + (b - a.b0)) * a.S + U.s] = U.A;
