@@ -514,62 +514,130 @@ __device__ __forceinline__ DF df_recip(int k) {
 }
 
 // Row (p, s, n) of the photon-mode binomial tables, pp = bpp[s] <= 1/2,
-// qq = 1 - pp, all in double-float: relative probabilities w(k) = pmf(k) /
-// pmf(m) around the mode m = min(floor((n+1) pp), n), upward w(k) =
-// w(k-1) * ((n-k+1) / k) * (pp/qq), downward w(k) = w(k+1) * ((k+1) / (n-k)) *
-// (qq/pp) (far tails underflow harmlessly to 0; FP32 cannot hold qq^n), the
-// total W summed upward then downward, then cdf[k] = float((sum_{i<=k} w(i)) *
-// (1/W)) clamped to 1 with cdf[n] = 1. guide[j] is the first k with
-// cdf[k] >= j/(n+1) (approximately; the draw corrects any start index).
-// One thread per row, 32-thread blocks so the rows spread over many SMs;
-// longest rows first.
-__global__ void binom_table_kernel(const DevParams *params, int P, int n_states, float *cdf_all,
-                                   uint16_t *guide_all) {
-    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+// qq = 1 - pp, in double-float, one warp per row (kTableLanes lanes):
+//  1. relative probabilities w(k) = pmf(k)/pmf(m) around the mode
+//     m = min(floor((n+1) pp), n): upward w(k) = w(k-1) * ((n-k+1)/k) * (pp/qq),
+//     downward w(k) = w(k+1) * ((k+1)/(n-k)) * (qq/pp). Each side is cut into
+//     kTableLanes contiguous chunks; a lane forms the running product inside
+//     its chunk, the chunk products are folded left to right across lanes,
+//     and w(k) = (product of the earlier chunks) * (running product), rounded
+//     to FP32 (far tails underflow harmlessly to 0);
+//  2. the cumulative sums of the FP32 w over k = 0..n, chunked the same way
+//     (chunk sums folded left to right; W = the fold of all chunks), and
+//     cdf[k] = float(cum(k) * (1/W)) clamped to 1, cdf[n] = 1;
+//  3. guide[j] = the first k with cdf[k] >= j/(n+1), by binary search.
+// The operation order is fixed, so the host reproduces the rows bit for bit.
+// Rows go longest first.
+constexpr int kTableLanes = 32;
+constexpr int kTableWarps = 8;
+
+__device__ __forceinline__ DF df_shfl(DF v, int src) {
+    return {__shfl_sync(0xffffffffu, v.hi, src), __shfl_sync(0xffffffffu, v.lo, src)};
+}
+
+__global__ void __launch_bounds__(kTableLanes * kTableWarps)
+binom_table_kernel(const DevParams *params, int P, int n_states, float *cdf_all, uint16_t *guide_all) {
+    __shared__ float s_hi[kTableWarps][kTableN + 1];
+    __shared__ float s_lo[kTableWarps][kTableN + 1];
+    const int lane = threadIdx.x & 31;
+    const int wl = threadIdx.x >> 5;
+    const int64_t rid = (int64_t)blockIdx.x * kTableWarps + wl;
     const int64_t total = (int64_t)P * n_states * (kTableN + 1);
-    if (tid >= total) return;
-    const int nn = kTableN - (int)(tid % (kTableN + 1));
-    const int s = (int)((tid / (kTableN + 1)) % n_states);
-    const int p = (int)(tid / ((int64_t)(kTableN + 1) * n_states));
+    if (rid >= total) return;                       // whole warps leave together
+    const int nn = kTableN - (int)(rid % (kTableN + 1));
+    const int s = (int)((rid / (kTableN + 1)) % n_states);
+    const int p = (int)(rid / ((int64_t)(kTableN + 1) * n_states));
     const size_t row = ((size_t)p * n_states + s) * kTableRows + (size_t)nn * (nn + 1) / 2;
     float *cdf = cdf_all + row;
     uint16_t *guide = guide_all + row;
+    float *hi = s_hi[wl];
+    float *lo = s_lo[wl];
     const float pp = params[p].bpp[s];
     const DF qq = df_fast_sum(1.0f, -pp);
     const DF up = df_div(pp, qq);
     const DF down = df_div2(qq, {pp, 0.0f});
     int m = (int)floorf((float)(nn + 1) * pp);
     if (m > nn) m = nn;
-    DF W = {1.0f, 0.0f};
-    cdf[m] = 1.0f;
-    DF w = {1.0f, 0.0f};
-#pragma unroll 4
-    for (int k = m + 1; k <= nn; ++k) {
-        w = df_mul(w, df_mul(df_mul({(float)(nn - k + 1), 0.0f}, df_recip(k)), up));
-        cdf[k] = w.hi + w.lo;
-        W = df_add(W, w);
+    // 1a. upward, k = m+1 .. nn
+    {
+        const int len = nn - m;
+        const int C = (len + kTableLanes - 1) / kTableLanes;
+        const int k0 = m + 1 + lane * C;
+        const int k1 = min(k0 + C - 1, nn);
+        DF w = {1.0f, 0.0f};
+        for (int k = k0; k <= k1; ++k) {
+            w = df_mul(w, df_mul(df_mul({(float)(nn - k + 1), 0.0f}, df_recip(k)), up));
+            hi[k] = w.hi;
+            lo[k] = w.lo;
+        }
+        DF Q = {1.0f, 0.0f};                        // product of the earlier chunks
+        for (int i = 0; i < kTableLanes; ++i) {
+            DF Pi = df_shfl(w, i);
+            if (i < lane) Q = df_mul(Q, Pi);
+        }
+        for (int k = k0; k <= k1; ++k) {
+            DF v = df_mul(Q, {hi[k], lo[k]});
+            hi[k] = v.hi + v.lo;
+        }
     }
-    w = {1.0f, 0.0f};
-#pragma unroll 4
-    for (int k = m - 1; k >= 0; --k) {
-        w = df_mul(w, df_mul(df_mul({(float)(k + 1), 0.0f}, df_recip(nn - k)), down));
-        cdf[k] = w.hi + w.lo;
-        W = df_add(W, w);
+    // 1b. downward, k = m-1 .. 0
+    {
+        const int len = m;
+        const int C = (len + kTableLanes - 1) / kTableLanes;
+        const int k0 = m - 1 - lane * C;
+        const int k1 = max(k0 - C + 1, 0);
+        DF w = {1.0f, 0.0f};
+        for (int k = k0; k >= k1; --k) {
+            w = df_mul(w, df_mul(df_mul({(float)(k + 1), 0.0f}, df_recip(nn - k)), down));
+            hi[k] = w.hi;
+            lo[k] = w.lo;
+        }
+        DF Q = {1.0f, 0.0f};
+        for (int i = 0; i < kTableLanes; ++i) {
+            DF Pi = df_shfl(w, i);
+            if (i < lane) Q = df_mul(Q, Pi);
+        }
+        for (int k = k0; k >= k1; --k) {
+            DF v = df_mul(Q, {hi[k], lo[k]});
+            hi[k] = v.hi + v.lo;
+        }
+    }
+    if (lane == 0) hi[m] = 1.0f;
+    __syncwarp();
+    // 2. cumulative sums of the FP32 w, chunked over k = 0..nn
+    const int C2 = (nn + 1 + kTableLanes - 1) / kTableLanes;
+    const int c0 = lane * C2;
+    const int c1 = min(c0 + C2, nn + 1);             // exclusive
+    DF T = {0.0f, 0.0f};
+    for (int k = c0; k < c1; ++k) T = df_add(T, {hi[k], 0.0f});
+    DF E = {0.0f, 0.0f}, W = {0.0f, 0.0f};           // sum of the earlier chunks; of all
+    for (int i = 0; i < kTableLanes; ++i) {
+        DF Ti = df_shfl(T, i);
+        if (i < lane) E = df_add(E, Ti);
+        W = df_add(W, Ti);
     }
     const DF invW = df_div(1.0f, W);
-    const float gstep = 1.0f / (float)(nn + 1);
-    int j = 0;
-    DF cum = {0.0f, 0.0f};
-#pragma unroll 4
-    for (int k = 0; k <= nn; ++k) {
-        cum = df_add(cum, {cdf[k], 0.0f});
+    DF cum = E;
+    for (int k = c0; k < c1; ++k) {
+        cum = df_add(cum, {hi[k], 0.0f});
         DF v = df_mul(cum, invW);
         float c = v.hi + v.lo;
         c = (k == nn) ? 1.0f : (c < 1.0f ? c : 1.0f);
+        lo[k] = c;
         cdf[k] = c;
-        while (j <= nn && (float)j * gstep <= c) guide[j++] = (uint16_t)k;
     }
-    while (j <= nn) guide[j++] = (uint16_t)nn;
+    __syncwarp();
+    // 3. guide: first k with cdf[k] >= j/(n+1) (cdf[nn] = 1 ends every search)
+    const float gstep = 1.0f / (float)(nn + 1);
+    for (int j = lane; j <= nn; j += kTableLanes) {
+        const float t = (float)j * gstep;
+        int a = 0, b = nn;
+        while (a < b) {
+            int mid = (a + b) >> 1;
+            if (lo[mid] >= t) b = mid; else a = mid + 1;
+        }
+        guide[j] = (uint16_t)a;
+    }
 }
 
 // ---------------------------------------------------------------- burst-store validation
@@ -611,7 +679,8 @@ cudaError_t launch_binom_tables(const DevParams *params, int P, int n_states, fl
                                 uint16_t *guide, cudaStream_t st) {
     const int64_t total = (int64_t)P * n_states * (kTableN + 1);
     if (total <= 0) return cudaSuccess;
-    binom_table_kernel<<<(unsigned)((total + 31) / 32), 32, 0, st>>>(params, P, n_states, cdf, guide);
+    binom_table_kernel<<<(unsigned)((total + kTableWarps - 1) / kTableWarps), kTableLanes * kTableWarps, 0, st>>>(
+        params, P, n_states, cdf, guide);
     return cudaGetLastError();
 }
 

@@ -373,6 +373,12 @@ static inline orc_df df_recip(int k) {
 /* CDF row of Binomial(nn, pp), pp <= 1/2, in double-float around the mode
  * (relative probabilities from w(m) = 1 upward then downward, total, running
  * sum times 1/total), clamped to 1 with out[nn] = 1, as the device builds it. */
+/* Row nn of the photon-mode table for pp <= 1/2, in the device's order
+ * (binom_table_kernel, one warp of TAB_LANES lanes per row): products of the
+ * ratios inside TAB_LANES contiguous chunks on each side of the mode, chunk
+ * products folded left to right, w(k) rounded to float; cumulative sums in
+ * TAB_LANES chunks over k = 0..nn, chunk sums folded left to right. */
+#define TAB_LANES 32
 static void binom_cdf_row_df(float pp, int nn, float *out) {
     orc_df qq = df_fast_sum(1.0f, -pp);
     orc_df up = df_div(pp, qq);
@@ -380,29 +386,81 @@ static void binom_cdf_row_df(float pp, int nn, float *out) {
     orc_df down = df_div2(qq, ppd);
     int m = (int)floorf((float)(nn + 1) * pp);
     if (m > nn) m = nn;
-    orc_df W = {1.0f, 0.0f}, w = {1.0f, 0.0f};
+    orc_df wl[ORC_TABLE_N + 1];
+    orc_df P[TAB_LANES];
+    /* upward, k = m+1 .. nn */
+    {
+        int len = nn - m, C = (len + TAB_LANES - 1) / TAB_LANES;
+        for (int l = 0; l < TAB_LANES; ++l) {
+            int k0 = m + 1 + l * C, k1 = k0 + C - 1 < nn ? k0 + C - 1 : nn;
+            orc_df w = {1.0f, 0.0f};
+            for (int k = k0; k <= k1; ++k) {
+                orc_df a = {(float)(nn - k + 1), 0.0f};
+                w = df_mul(w, df_mul(df_mul(a, df_recip(k)), up));
+                wl[k] = w;
+            }
+            P[l] = w;
+        }
+        for (int l = 0; l < TAB_LANES; ++l) {
+            orc_df Q = {1.0f, 0.0f};
+            for (int i = 0; i < l; ++i) Q = df_mul(Q, P[i]);
+            int k0 = m + 1 + l * C, k1 = k0 + C - 1 < nn ? k0 + C - 1 : nn;
+            for (int k = k0; k <= k1; ++k) {
+                orc_df v = df_mul(Q, wl[k]);
+                out[k] = v.hi + v.lo;
+            }
+        }
+    }
+    /* downward, k = m-1 .. 0 */
+    {
+        int len = m, C = (len + TAB_LANES - 1) / TAB_LANES;
+        for (int l = 0; l < TAB_LANES; ++l) {
+            int k0 = m - 1 - l * C, k1 = k0 - C + 1 > 0 ? k0 - C + 1 : 0;
+            orc_df w = {1.0f, 0.0f};
+            for (int k = k0; k >= k1; --k) {
+                orc_df a = {(float)(k + 1), 0.0f};
+                w = df_mul(w, df_mul(df_mul(a, df_recip(nn - k)), down));
+                wl[k] = w;
+            }
+            P[l] = w;
+        }
+        for (int l = 0; l < TAB_LANES; ++l) {
+            orc_df Q = {1.0f, 0.0f};
+            for (int i = 0; i < l; ++i) Q = df_mul(Q, P[i]);
+            int k0 = m - 1 - l * C, k1 = k0 - C + 1 > 0 ? k0 - C + 1 : 0;
+            for (int k = k0; k >= k1; --k) {
+                orc_df v = df_mul(Q, wl[k]);
+                out[k] = v.hi + v.lo;
+            }
+        }
+    }
     out[m] = 1.0f;
-    for (int k = m + 1; k <= nn; ++k) {
-        orc_df a = {(float)(nn - k + 1), 0.0f};
-        w = df_mul(w, df_mul(df_mul(a, df_recip(k)), up));
-        out[k] = w.hi + w.lo;
-        W = df_add(W, w);
+    /* cumulative sums */
+    int C2 = (nn + 1 + TAB_LANES - 1) / TAB_LANES;
+    orc_df T[TAB_LANES];
+    for (int l = 0; l < TAB_LANES; ++l) {
+        int c0 = l * C2, c1 = c0 + C2 < nn + 1 ? c0 + C2 : nn + 1;
+        orc_df t = {0.0f, 0.0f};
+        for (int k = c0; k < c1; ++k) {
+            orc_df x = {out[k], 0.0f};
+            t = df_add(t, x);
+        }
+        T[l] = t;
     }
-    w.hi = 1.0f; w.lo = 0.0f;
-    for (int k = m - 1; k >= 0; --k) {
-        orc_df a = {(float)(k + 1), 0.0f};
-        w = df_mul(w, df_mul(df_mul(a, df_recip(nn - k)), down));
-        out[k] = w.hi + w.lo;
-        W = df_add(W, w);
-    }
+    orc_df W = {0.0f, 0.0f};
+    for (int i = 0; i < TAB_LANES; ++i) W = df_add(W, T[i]);
     orc_df invW = df_div(1.0f, W);
-    orc_df cum = {0.0f, 0.0f};
-    for (int k = 0; k <= nn; ++k) {
-        orc_df t = {out[k], 0.0f};
-        cum = df_add(cum, t);
-        orc_df v = df_mul(cum, invW);
-        float c = v.hi + v.lo;
-        out[k] = (k == nn) ? 1.0f : (c < 1.0f ? c : 1.0f);
+    for (int l = 0; l < TAB_LANES; ++l) {
+        orc_df cum = {0.0f, 0.0f};
+        for (int i = 0; i < l; ++i) cum = df_add(cum, T[i]);
+        int c0 = l * C2, c1 = c0 + C2 < nn + 1 ? c0 + C2 : nn + 1;
+        for (int k = c0; k < c1; ++k) {
+            orc_df x = {out[k], 0.0f};
+            cum = df_add(cum, x);
+            orc_df v = df_mul(cum, invW);
+            float c = v.hi + v.lo;
+            out[k] = (k == nn) ? 1.0f : (c < 1.0f ? c : 1.0f);
+        }
     }
 }
 
