@@ -61,7 +61,7 @@ struct gpda_ctx {
     int32_t *dUnit = nullptr;
     size_t cap_unit = 0;
     float *dCdf = nullptr;          // photon-mode binomial tables
-    uint16_t *dGuide = nullptr;
+    GuideEntry *dGuide = nullptr;
     size_t cap_tab = 0;             // in (parameter set, state) tables
     // expected-histogram path
     ExpParams *dExp = nullptr;
@@ -214,14 +214,14 @@ int do_launch(gpda_ctx *c, int mode, int P, int n, const float *params, int64_t 
             free_dev(c->dGuide);
             c->dCdf = nullptr; c->dGuide = nullptr; c->cap_tab = 0;
             CK(cudaMalloc(&c->dCdf, sizeof(float) * kTableRows * ntab));
-            CK(cudaMalloc(&c->dGuide, sizeof(uint16_t) * kTableRows * ntab));
+            CK(cudaMalloc(&c->dGuide, sizeof(GuideEntry) * kTableRows * ntab));
             c->cap_tab = ntab;
         }
         CK(launch_binom_tables(c->dParams, P, n, c->dCdf, c->dGuide, c->stream));
         c->launches += 1;
     }
     CK(cudaMemsetAsync(c->dHist, 0, sizeof(unsigned long long) * (size_t)P * nbins, c->stream));
-    CK(cudaMemsetAsync(c->dWork, 0, sizeof(unsigned int), c->stream));
+    CK(cudaMemsetAsync(c->dWork, 0, 2 * sizeof(unsigned int), c->stream));
     c->last_P = P;
     c->last_chi2 = false;
     if (b1 == b0) return GPDA_OK;
@@ -255,6 +255,13 @@ int do_launch(gpda_ctx *c, int mode, int P, int n, const float *params, int64_t 
     a.r0 = c->model.r0;
     a.bg_a = c->model.bg_a;
     a.bg_d = c->model.bg_d;
+    if (c->has_obs) {        // chi-square in the kernel's last CTA
+        a.obs = c->dObs;
+        a.chi2 = c->dChi2;
+        a.done = c->dWork + 1;
+        a.left_pad = c->model.left_pad;
+        a.n_states = n;
+    }
     size_t dyn = (mode == GPDA_MODE_PHOTON) ? sizeof(float) * kSmemCapFloats : 0;
     int grid = std::min<int64_t>(a.n_items, (int64_t)c->num_sms * c->blocks_per_sm[mode]);
     CK(cudaEventRecord(c->k0, c->stream));
@@ -262,11 +269,7 @@ int do_launch(gpda_ctx *c, int mode, int P, int n, const float *params, int64_t 
     CK(cudaEventRecord(c->k1, c->stream));
     c->timed = true;
     c->launches += 1;
-    if (c->has_obs) {
-        CK(launch_chi2(c->dHist, c->dObs, P, nbins, c->model.left_pad, S, n, c->dChi2, c->stream));
-        c->launches += 1;
-        c->last_chi2 = true;
-    }
+    c->last_chi2 = c->has_obs;
     return GPDA_OK;
 }
 
@@ -472,7 +475,7 @@ gpda_ctx *gpda_create(int32_t device, const gpda_model *m, int32_t *status) {
     if (bad(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking))) return nullptr;
     if (bad(cudaEventCreateWithFlags(&c->params_ev, cudaEventDisableTiming))) return nullptr;
     if (bad(cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device))) return nullptr;
-    if (bad(cudaMalloc(&c->dWork, sizeof(unsigned int)))) return nullptr;
+    if (bad(cudaMalloc(&c->dWork, 2 * sizeof(unsigned int)))) return nullptr;   // work items, CTAs done
     if (bad(cudaMalloc(&c->dLimit, sizeof(unsigned long long)))) return nullptr;
     if (bad(cudaMemset(c->dLimit, 0, sizeof(unsigned long long)))) return nullptr;
     if (bad(cudaMalloc(&c->dObs, sizeof(float) * GPDA_MAX_BINS))) return nullptr;
@@ -755,7 +758,7 @@ int32_t gpda_graph_create(gpda_ctx *c, int32_t mode, int32_t P, int32_t n, int32
         free_dev(c->dGuide);
         c->dCdf = nullptr; c->dGuide = nullptr; c->cap_tab = 0;
         CK(cudaMalloc(&c->dCdf, sizeof(float) * kTableRows * (size_t)P * n));
-        CK(cudaMalloc(&c->dGuide, sizeof(uint16_t) * kTableRows * (size_t)P * n));
+        CK(cudaMalloc(&c->dGuide, sizeof(GuideEntry) * kTableRows * (size_t)P * n));
         c->cap_tab = (size_t)P * n;
     }
     const int nbins = c->model.nbins;
@@ -772,6 +775,10 @@ int32_t gpda_graph_create(gpda_ctx *c, int32_t mode, int32_t P, int32_t n, int32
     a.smem_cap = kSmemCapFloats; a.pbase = 0u;
     a.gamma = c->model.gamma; a.ct = c->model.crosstalk; a.r0 = c->model.r0;
     a.bg_a = c->model.bg_a; a.bg_d = c->model.bg_d;
+    if (c->has_obs) {
+        a.obs = c->dObs; a.chi2 = c->dChi2; a.done = c->dWork + 1;
+        a.left_pad = c->model.left_pad; a.n_states = n;
+    }
     const size_t dyn = (mode == GPDA_MODE_PHOTON) ? sizeof(float) * kSmemCapFloats : 0;
     const int grid = (int)std::min<int64_t>(a.n_items, (int64_t)c->num_sms * c->blocks_per_sm[mode]);
     // one stream capture of the whole batched step
@@ -780,9 +787,8 @@ int32_t gpda_graph_create(gpda_ctx *c, int32_t mode, int32_t P, int32_t n, int32
     cudaError_t e = cudaMemcpyAsync(c->dParams, c->hParams, sizeof(DevParams) * P, cudaMemcpyHostToDevice, c->stream);
     if (e == cudaSuccess && mode == GPDA_MODE_PHOTON) { e = launch_binom_tables(c->dParams, P, n, c->dCdf, c->dGuide, c->stream); kernels++; }
     if (e == cudaSuccess) e = cudaMemsetAsync(c->dHist, 0, sizeof(unsigned long long) * (size_t)P * nbins, c->stream);
-    if (e == cudaSuccess) e = cudaMemsetAsync(c->dWork, 0, sizeof(unsigned int), c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->dWork, 0, 2 * sizeof(unsigned int), c->stream);
     if (e == cudaSuccess) { e = launch_pda(mode, a, grid, dyn, c->stream); kernels++; }
-    if (e == cudaSuccess && c->has_obs) { e = launch_chi2(c->dHist, c->dObs, P, nbins, c->model.left_pad, S, n, c->dChi2, c->stream); kernels++; }
     if (e == cudaSuccess) e = cudaMemcpyAsync(c->hHist, c->dHist, sizeof(unsigned long long) * (size_t)P * nbins, cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess && c->has_obs) e = cudaMemcpyAsync(c->hChi2, c->dChi2, sizeof(double) * P, cudaMemcpyDeviceToHost, c->stream);
     cudaGraph_t g = nullptr;

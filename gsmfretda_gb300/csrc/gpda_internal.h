@@ -57,9 +57,15 @@ constexpr int kParamWords = (int)(sizeof(DevParams) / 4);
 constexpr int kTableN = GPDA_TABLE_N;
 constexpr int kTableRows = (kTableN + 1) * (kTableN + 2) / 2;   // entries per (parameter set, state)
 
+// Photon-mode guide entry for cell j of a table row: the first k with
+// cdf[k] >= j/(n+1) (x) and the bits of cdf[k-1] (w; -1 for k = 0), cdf[k]
+// (y) and cdf[k+1] (z; 2 for k = n), so that one 16-byte load settles almost
+// every draw.
+using GuideEntry = uint4;
+
 struct PdaArgs {
     const float *bcdf;            // photon mode: CDF rows, P * n_states * kTableRows
-    const uint16_t *bguide;       // photon mode: guide rows, same indexing
+    const GuideEntry *bguide;     // photon mode: guide rows, same indexing
     const int32_t *N;
     const float *T;
     const int64_t *off_idx;
@@ -80,6 +86,12 @@ struct PdaArgs {
     int32_t smem_cap;             // photon staging capacity (floats)
     uint32_t pbase;               // parameter-set word of the counter = pbase + p
     float gamma, ct, r0, bg_a, bg_d;
+    // reduced chi-square in the kernel's last CTA (chi2 null: none)
+    const float *obs;             // nbins observed counts
+    double *chi2;                 // P
+    unsigned int *done;           // CTAs finished, zeroed before launch
+    int32_t left_pad;
+    int32_t n_states;
 };
 
 struct RcArgs {
@@ -107,7 +119,7 @@ cudaError_t launch_chi2(const unsigned long long *hist, const float *obs, int P,
                         int left_pad, int S, int n_states, double *chi2, cudaStream_t st);
 cudaError_t launch_rc(const RcArgs &a, cudaStream_t st);
 cudaError_t launch_binom_tables(const DevParams *params, int P, int n_states, float *cdf,
-                                uint16_t *guide, cudaStream_t st);
+                                GuideEntry *guide, cudaStream_t st);
 cudaError_t launch_validate(const int32_t *N, const float *T, const int64_t *off_idx,
                             const float *offsets, int64_t B, unsigned int *flag, int num_sms,
                             cudaStream_t st);

@@ -76,7 +76,7 @@ __device__ __forceinline__ int next_state(const Unit &U, const DevParams &P, flo
 // tabulated CDF of Binomial(n, min(eps, 1-eps)): the smallest k with
 // u <= cdf[k] (cdf[n] = 1); larger n fall back to BINV/BTRD.
 __device__ __forceinline__ int binom_table(Rng &r, int n, const DevParams &P, int st,
-                                           const float *cdf_p, const uint16_t *guide_p, int &lim,
+                                           const float *cdf_p, const GuideEntry *guide_p, int &lim,
                                            const float *inv) {
     const float p = P.eps[st];
     if (n <= 0 || !(p > 0.0f)) return 0;
@@ -88,9 +88,18 @@ __device__ __forceinline__ int binom_table(Rng &r, int n, const DevParams &P, in
     const float u = r.u01();
     int j = (int)(u * (float)(n + 1));
     if (j > n) j = n;
-    int k = guide_p[row + j];
-    while (k > 0 && u <= __ldg(cdf + k - 1)) --k;
-    while (k < n && u > __ldg(cdf + k)) ++k;
+    const GuideEntry e = __ldg(guide_p + row + j);
+    int k = (int)e.x;
+    if (u <= __uint_as_float(e.w)) {                 // rounding of j: below the start
+        k -= 1;
+        while (k > 0 && u <= __ldg(cdf + k - 1)) --k;
+    } else if (u > __uint_as_float(e.y)) {
+        k += 1;
+        if (u > __uint_as_float(e.z)) {
+            k += 1;
+            while (k < n && u > __ldg(cdf + k)) ++k;
+        }
+    }
     return flip ? n - k : k;
 }
 
@@ -102,7 +111,7 @@ __device__ __forceinline__ int binom_table(Rng &r, int n, const DevParams &P, in
 __device__ __forceinline__ bool step_pho(Unit &U, const DevParams &P, const float *offs, float g,
                                          float ct, float r0, float bga, float bgd, int &lim,
                                          const float *inv, const float *cdf_p,
-                                         const uint16_t *guide_p) {
+                                         const GuideEntry *guide_p) {
     U.r.align_now();   // the state draw follows at once
     const int st = next_state(U, P, U.r.u01());
     U.st = st;
@@ -184,6 +193,43 @@ __device__ __forceinline__ void hist_add(unsigned int *sh, int bin) {
     unsigned peers = __match_any_sync(mask, bin);
     int leader = __ffs(peers) - 1;
     if ((int)(threadIdx.x & 31) == leader && bin >= 0) atomicAdd(&sh[bin], (unsigned)__popc(peers));
+}
+
+// Reduced chi-square of parameter set p (src/streamWorker.cpp:197-206), FP64,
+// sequential over bins; the counts are read past L1 (__ldcg), since other
+// CTAs wrote them with atomics.
+__device__ __forceinline__ double chi2_of(const unsigned long long *h, const float *obs, int nbins,
+                                          int left_pad, int S, int n_states) {
+    int effN = nbins - left_pad;
+    double chi = 0.0;
+    for (int i = left_pad; i < nbins; ++i) {
+        const unsigned long long c = __ldcg(h + i);
+        if (c > 0ull) {
+            double mi = (double)c / (double)S;
+            double d = (double)obs[i] - mi;
+            chi = chi + d * d / mi;
+        } else {
+            effN -= 1;
+        }
+    }
+    return chi / (double)(effN - n_states * (n_states + 1));
+}
+
+// the last CTA to finish computes every parameter set's chi-square (no CTA
+// waits: each counts itself once, after its own atomics); out of line so that
+// the simulation loop's registers are not shaped by it
+static __device__ __noinline__ void last_cta_chi2(const PdaArgs &a) {
+    __shared__ int s_last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = (atomicAdd(a.done, 1u) == gridDim.x - 1) ? 1 : 0;
+    __syncthreads();
+    if (s_last) {
+        __threadfence();
+        for (int q = threadIdx.x; q < a.P; q += kThreads)
+            a.chi2[q] = chi2_of(a.hist + (size_t)q * a.nbins, a.obs, a.nbins, a.left_pad, a.S,
+                                a.n_states);
+    }
 }
 
 template <int MODE>
@@ -311,6 +357,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) pda_kernel(const PdaArgs
         }
     }
     if (lim) atomicAdd(a.limit_hits, (unsigned long long)lim);
+    if (a.chi2) last_cta_chi2(a);
 }
 
 __global__ void chi2_kernel(const unsigned long long *hist, const float *obs, int P, int nbins,
@@ -536,7 +583,7 @@ __device__ __forceinline__ DF df_shfl(DF v, int src) {
 }
 
 __global__ void __launch_bounds__(kTableLanes * kTableWarps)
-binom_table_kernel(const DevParams *params, int P, int n_states, float *cdf_all, uint16_t *guide_all) {
+binom_table_kernel(const DevParams *params, int P, int n_states, float *cdf_all, GuideEntry *guide_all) {
     __shared__ float s_hi[kTableWarps][kTableN + 1];
     __shared__ float s_lo[kTableWarps][kTableN + 1];
     const int lane = threadIdx.x & 31;
@@ -549,7 +596,7 @@ binom_table_kernel(const DevParams *params, int P, int n_states, float *cdf_all,
     const int p = (int)(rid / ((int64_t)(kTableN + 1) * n_states));
     const size_t row = ((size_t)p * n_states + s) * kTableRows + (size_t)nn * (nn + 1) / 2;
     float *cdf = cdf_all + row;
-    uint16_t *guide = guide_all + row;
+    GuideEntry *guide = guide_all + row;
     float *hi = s_hi[wl];
     float *lo = s_lo[wl];
     const float pp = params[p].bpp[s];
@@ -627,7 +674,8 @@ binom_table_kernel(const DevParams *params, int P, int n_states, float *cdf_all,
         cdf[k] = c;
     }
     __syncwarp();
-    // 3. guide: first k with cdf[k] >= j/(n+1) (cdf[nn] = 1 ends every search)
+    // 3. guide entries: first k with cdf[k] >= j/(n+1) (cdf[nn] = 1 ends every
+    //    search) and its neighbouring cdf values
     const float gstep = 1.0f / (float)(nn + 1);
     for (int j = lane; j <= nn; j += kTableLanes) {
         const float t = (float)j * gstep;
@@ -636,7 +684,9 @@ binom_table_kernel(const DevParams *params, int P, int n_states, float *cdf_all,
             int mid = (a + b) >> 1;
             if (lo[mid] >= t) b = mid; else a = mid + 1;
         }
-        guide[j] = (uint16_t)a;
+        const float cm = a > 0 ? lo[a - 1] : -1.0f;
+        const float c1 = a < nn ? lo[a + 1] : 2.0f;
+        guide[j] = make_uint4((unsigned)a, __float_as_uint(lo[a]), __float_as_uint(c1), __float_as_uint(cm));
     }
 }
 
@@ -676,7 +726,7 @@ __global__ void validate_kernel(const int32_t *N, const float *T, const int64_t 
 // ---------------------------------------------------------------- launchers
 
 cudaError_t launch_binom_tables(const DevParams *params, int P, int n_states, float *cdf,
-                                uint16_t *guide, cudaStream_t st) {
+                                GuideEntry *guide, cudaStream_t st) {
     const int64_t total = (int64_t)P * n_states * (kTableN + 1);
     if (total <= 0) return cudaSuccess;
     binom_table_kernel<<<(unsigned)((total + kTableWarps - 1) / kTableWarps), kTableLanes * kTableWarps, 0, st>>>(

@@ -12,7 +12,7 @@
 // loop-limit counter) lives in one fixed array inside this library.
 //
 // The array is a file-scope __device__ array of kNoAllocScratchBytes bytes
-// (about 6.4 MB): every device that loads the library holds a copy until the
+// (about 21 MB): every device that loads the library holds a copy until the
 // process exits. It limits a call to kNoAllocMaxP (64) parameter sets, and in
 // photon mode to kNoAllocMaxTables (8) parameter-set x state binomial tables
 // (P * n_states <= 8).
@@ -46,7 +46,7 @@ struct NoAllocScratch {
     unsigned int pad_[3];
     unsigned long long limit_hits;
     float cdf[kNoAllocMaxTables * kTableRows];
-    uint16_t guide[kNoAllocMaxTables * kTableRows];
+    GuideEntry guide[kNoAllocMaxTables * kTableRows];
 };
 constexpr size_t kNoAllocScratchBytes = sizeof(NoAllocScratch);
 

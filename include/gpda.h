@@ -214,7 +214,7 @@ int32_t gpda_expected_grad(gpda_ctx *ctx, int32_t P, int32_t n_states, const flo
  * array hist (zeroed first); with ohist/chi2 (device, nbins floats / P
  * doubles) it also writes the reduced chi-square. params is a HOST array of
  * P*n(n+1) floats. Allocates nothing: its scratch is a fixed array of about
- * 6.4 MB inside the library, held by every device that loads it until exit,
+ * 21 MB inside the library, held by every device that loads it until exit,
  * which limits P to 64, and in photon mode P*n_states to 8 (GPDA_ERR_ARG
  * beyond). Runs asynchronously on `stream`
  * (a cudaStream_t, NULL = legacy default stream) on the current device.
