@@ -109,13 +109,15 @@ __device__ __forceinline__ float binom_pmf(int n, int m, float p, float q) {
     return expf_(lc) * sqrtf(fn * inv2pi / ((float)m * (float)(n - m)));
 }
 
-// first acceptor count a with floor(a * nbins / N) >= b
+// first acceptor count a with floor(a * nbins / N) >= b. The store holds
+// N <= 2^21 photons per burst and this path nbins <= 64, so every product
+// below stays under 2^27: 32-bit unsigned division is exact.
 __device__ __forceinline__ int bin_start(int b, int N, int nbins) {
-    return (int)(((int64_t)b * N + nbins - 1) / nbins);
+    return (int)(((unsigned)b * (unsigned)N + (unsigned)(nbins - 1)) / (unsigned)nbins);
 }
 
 __device__ __forceinline__ int bin_of(int a, int N, int nbins) {
-    int b = (int)(((int64_t)a * nbins) / N);
+    int b = (int)(((unsigned)a * (unsigned)nbins) / (unsigned)N);
     return b < nbins - 1 ? b : nbins - 1;
 }
 
@@ -322,10 +324,12 @@ __global__ void __launch_bounds__(kExpThreads) exp_fwd_kernel(const ExpArgs a) {
     __syncthreads();
     const int64_t units = a.B * (int64_t)a.S;
     const int64_t stride = (int64_t)a.nblk * kExpThreads;
+    const bool narrow = units + stride <= (int64_t)0xffffffffu;
     int lim = 0;
     float *row = sh_rows + tid;
     for (int64_t u = (int64_t)blockIdx.x * kExpThreads + tid; u < units; u += stride) {
-        const int b = (int)(u / a.S);
+        // (32-bit division whenever the unit count allows)
+        const int b = narrow ? (int)((uint32_t)u / (uint32_t)a.S) : (int)(u / a.S);
         const int s = (int)(u - (int64_t)b * a.S);
         const int Nb = __ldg(a.N + b);
         const float Tb = __ldg(a.T + b);
@@ -426,9 +430,11 @@ __global__ void __launch_bounds__(kExpThreads) exp_adj_kernel(const ExpArgs a) {
     for (int k = 0; k < NG; ++k) gacc[k] = 0.0f;
     const int64_t units = a.B * (int64_t)a.S;
     const int64_t stride = (int64_t)a.nblk_adj * kExpThreads;
+    const bool narrow = units + stride <= (int64_t)0xffffffffu;
     int lim = 0;
     for (int64_t u = (int64_t)blockIdx.x * kExpThreads + tid; u < units; u += stride) {
-        const int b = (int)(u / a.S);
+        // (32-bit division whenever the unit count allows)
+        const int b = narrow ? (int)((uint32_t)u / (uint32_t)a.S) : (int)(u / a.S);
         const int s = (int)(u - (int64_t)b * a.S);
         const int Nb = __ldg(a.N + b);
         const float Tb = __ldg(a.T + b);
