@@ -168,6 +168,30 @@ __device__ __forceinline__ bool traj_occ(Unit &U, const DevParams &P, float r0, 
     return false;
 }
 
+// The occupancy split draws its background through out-of-line Poisson
+// samplers: measured 3-5 % faster there (the split runs once per unit),
+// while the photon step keeps them inline (out of line costs it 40 %).
+static __device__ __noinline__ int pinv_ool(Rng &r, float lam, int &lim, const float *inv) {
+    return pinv(r, lam, lim, inv);
+}
+static __device__ __noinline__ int ptrs_ool(Rng &r, float lam, int &lim) { return ptrs(r, lam, lim); }
+
+__device__ __forceinline__ int background_occ(Rng &r, int navail, float lam_a, float lam_d, int *sig,
+                                              int &lim, const float *inv) {
+    int B[2];
+    int avail = navail;
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+        const float lam = c == 0 ? lam_a : lam_d;
+        int x = !(lam > 0.0f) ? 0 : (lam < 10.0f) ? pinv_ool(r, lam, lim, inv) : ptrs_ool(r, lam, lim);
+        if (x > avail) x = (int)floorf((float)avail * r.u01());
+        B[c] = x;
+        avail -= x;
+    }
+    *sig = avail;
+    return B[0];
+}
+
 // Occupancy mode, after the trajectory: a fresh block for the background and
 // the single binomial split with the occupancy-weighted efficiency.
 __device__ __forceinline__ void final_occ(Unit &U, const DevParams &P, float g, float ct, float bga,
@@ -175,7 +199,7 @@ __device__ __forceinline__ void final_occ(Unit &U, const DevParams &P, float g, 
     float eeff = (U.Tb > 0.0f) ? U.acc / U.Tb : P.E[U.st];
     U.r.align();
     int sig;
-    int ba = background(U.r, U.Nb, bga * U.Tb, bgd * U.Tb, &sig, lim, inv);
+    int ba = background_occ(U.r, U.Nb, bga * U.Tb, bgd * U.Tb, &sig, lim, inv);
     U.A = binom(U.r, sig, eps_of(eeff, g, ct), lim, inv) + ba;
 }
 
