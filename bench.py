@@ -13,8 +13,9 @@ samples per burst, fused 21-bin histogram + FP64 reduced chi-square.
 value: device-timed throughput with the burst store resident in HBM (CUDA
 events on the engine stream around each step; a 256 MB write flushes the L2
 between steps, outside the events). e2e: the same metric through the C ABI
-with pinned HOST buffers: each step uploads the burst store (+ device-side
-validation) and the parameters, runs, and reads back histogram + chi-square.
+with pinned HOST buffers: each step is one gpda_run_host call, which copies
+the burst store in two ranges (validated on the device) overlapped with the
+simulation, and reads back histogram + chi-square.
 
 --impl reference times the CPU restatement of the path (the reference has no
 CPU Monte-Carlo of its own) on the host cores of this machine, all threads.
@@ -579,8 +580,9 @@ def main():
         l2_flush()
         eng.synchronize()
         t0 = time.perf_counter()
-        eng.upload(N=hN, T=hT, off_idx=hOI, offsets=hOF)
-        h, c2 = eng.run_plain(MODE_PHOTON, n, hA, S, 30_000 + k)
+        # one C-ABI call: the store's copy overlapped with the simulation
+        h, c2 = eng.run_host(MODE_PHOTON, n, hA, S, 30_000 + k, N=hN, T=hT, off_idx=hOI,
+                             offsets=hOF, ranges=2)
         t1 = time.perf_counter()
         if k >= 2:
             e2e_s.append(t1 - t0)

@@ -57,6 +57,8 @@ SIGNATURES = {
     "gpda_launch_count": (_I64, [_VP]),
     "gpda_limit_hits": (_I64, [_VP]),
     "gpda_kernel_ms": (_F, [_VP]),
+    "gpda_run_host": (_I32, [_VP, _I32, _I32, _I32, _VP, _VP, _VP, _VP, _VP, _I64, _I32, _U64, _I32,
+                             _VP, _VP]),
     "gpda_graph_create": (_I32, [_VP, _I32, _I32, _I32, _I32]),
     "gpda_graph_run": (_I32, [_VP, _VP, _U64, _VP, _VP]),
     "gpda_autotune": (_I32, [_VP, _I32, _I32, _I32, _VP, _I32, _U64, _VP]),

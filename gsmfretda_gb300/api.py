@@ -120,6 +120,27 @@ class Engine:
                                        _p(units), _p(hist)), self.ctx)
         return units, hist
 
+    def run_host(self, mode, n, args, samples, seed, bs=None, N=None, T=None, off_idx=None,
+                 offsets=None, ranges=4):
+        """Upload the bursts and run all parameter sets in one call, the copy
+        overlapped with the simulation (ranges of bursts); the store stays
+        uploaded. Returns hist (P, nbins) and chi2 (P,)."""
+        if bs is not None:
+            N, T, off_idx, offsets = bs.N, bs.T, bs.off_idx, bs.offsets
+        N = np.ascontiguousarray(N, dtype=np.int32)
+        T = np.ascontiguousarray(T, dtype=np.float32)
+        oi = None if off_idx is None else np.ascontiguousarray(off_idx, dtype=np.int64)
+        of = None if offsets is None else np.ascontiguousarray(offsets, dtype=np.float32)
+        a = np.ascontiguousarray(args, dtype=np.float32).reshape(-1)
+        P = a.size // (n * (n + 1))
+        hist = np.zeros((P, self.nbins), dtype=np.uint64)
+        chi2 = np.zeros(P, dtype=np.float64)
+        rc = self.lib.gpda_run_host(self.ctx, mode, P, n, _p(a), _p(N), _p(T), _p(oi), _p(of), N.size,
+                                    samples, seed, ranges, _p(hist), _p(chi2))
+        self.B = N.size if rc == GPDA_OK else 0
+        _check(rc, self.ctx)
+        return hist, chi2
+
     # ---------------------------------------------------------------- captured launch
     def graph_create(self, mode, n, P, samples):
         """Capture one batched step (P parameter sets) as a CUDA graph."""

@@ -26,7 +26,9 @@ using namespace gpda;
 struct gpda_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t cstream = nullptr;      // copies of gpda_run_host
     cudaEvent_t params_ev = nullptr;
+    std::vector<cudaEvent_t> range_ev;   // one per burst range of gpda_run_host
     gpda_model model{};
     int num_sms = 0;
     // burst store
@@ -183,15 +185,8 @@ void free_graph(gpda_ctx *c) {
     c->g_P = 0;
 }
 
-int do_launch(gpda_ctx *c, int mode, int P, int n, const float *params, int64_t b0, int64_t b1,
-              int S, uint64_t seed, int32_t *dUnit) {
-    if (mode != GPDA_MODE_OCCUPANCY && mode != GPDA_MODE_PHOTON) return fail(c, GPDA_ERR_ARG, "mode");
-    if (P < 1 || n < 1 || n > GPDA_MAX_STATES || S < 1 || !params) return fail(c, GPDA_ERR_ARG, "P, n_states, samples or params");
-    if (c->B == 0 || !c->dN) return fail(c, GPDA_ERR_STATE, "no bursts uploaded");
-    if (b0 < 0 || b1 < b0 || b1 > c->B) return fail(c, GPDA_ERR_ARG, "burst range");
-    if (mode == GPDA_MODE_PHOTON && !c->has_offsets) return fail(c, GPDA_ERR_STATE, "photon mode needs arrival offsets");
-    if ((int64_t)(b1 - b0) * S > (int64_t)INT32_MAX) return fail(c, GPDA_ERR_ARG, "too many units per parameter set");
-    CK(cudaSetDevice(c->device));
+// Parameters to the device, photon tables, histogram reset (stream-ordered).
+int prepare_launch(gpda_ctx *c, int mode, int P, int n, const float *params) {
     int rc = ensure_scratch(c, P);
     if (rc) return rc;
     // the pinned parameter staging may still be read by the previous copy
@@ -221,9 +216,17 @@ int do_launch(gpda_ctx *c, int mode, int P, int n, const float *params, int64_t 
         c->launches += 1;
     }
     CK(cudaMemsetAsync(c->dHist, 0, sizeof(unsigned long long) * (size_t)P * nbins, c->stream));
-    CK(cudaMemsetAsync(c->dWork, 0, 2 * sizeof(unsigned int), c->stream));
     c->last_P = P;
     c->last_chi2 = false;
+    return GPDA_OK;
+}
+
+// The Monte-Carlo kernel over bursts [b0, b1) of all P parameter sets, adding
+// into the histogram; with_chi2: the kernel's last CTA also writes the
+// chi-square; abort_flag: see PdaArgs.
+int enqueue_range(gpda_ctx *c, int mode, int P, int n, int64_t b0, int64_t b1, int S,
+                  uint64_t seed, int32_t *dUnit, bool with_chi2, const unsigned int *abort_flag) {
+    CK(cudaMemsetAsync(c->dWork, 0, 2 * sizeof(unsigned int), c->stream));
     if (b1 == b0) return GPDA_OK;
     PdaArgs a{};
     a.bcdf = c->dCdf;
@@ -247,7 +250,7 @@ int do_launch(gpda_ctx *c, int mode, int P, int n, const float *params, int64_t 
     if (ntiles * P > (int64_t)INT32_MAX) return fail(c, GPDA_ERR_ARG, "too many work items");
     a.ntiles = (int)ntiles;
     a.n_items = (int)(ntiles * P);
-    a.nbins = nbins;
+    a.nbins = c->model.nbins;
     a.smem_cap = kSmemCapFloats;
     a.pbase = 0u;
     a.gamma = c->model.gamma;
@@ -255,13 +258,14 @@ int do_launch(gpda_ctx *c, int mode, int P, int n, const float *params, int64_t 
     a.r0 = c->model.r0;
     a.bg_a = c->model.bg_a;
     a.bg_d = c->model.bg_d;
-    if (c->has_obs) {        // chi-square in the kernel's last CTA
+    if (with_chi2) {        // chi-square in the kernel's last CTA
         a.obs = c->dObs;
         a.chi2 = c->dChi2;
         a.done = c->dWork + 1;
         a.left_pad = c->model.left_pad;
         a.n_states = n;
     }
+    a.abort_flag = abort_flag;
     size_t dyn = (mode == GPDA_MODE_PHOTON) ? sizeof(float) * kSmemCapFloats : 0;
     int grid = std::min<int64_t>(a.n_items, (int64_t)c->num_sms * c->blocks_per_sm[mode]);
     CK(cudaEventRecord(c->k0, c->stream));
@@ -269,8 +273,22 @@ int do_launch(gpda_ctx *c, int mode, int P, int n, const float *params, int64_t 
     CK(cudaEventRecord(c->k1, c->stream));
     c->timed = true;
     c->launches += 1;
-    c->last_chi2 = c->has_obs;
+    c->last_chi2 = with_chi2;
     return GPDA_OK;
+}
+
+int do_launch(gpda_ctx *c, int mode, int P, int n, const float *params, int64_t b0, int64_t b1,
+              int S, uint64_t seed, int32_t *dUnit) {
+    if (mode != GPDA_MODE_OCCUPANCY && mode != GPDA_MODE_PHOTON) return fail(c, GPDA_ERR_ARG, "mode");
+    if (P < 1 || n < 1 || n > GPDA_MAX_STATES || S < 1 || !params) return fail(c, GPDA_ERR_ARG, "P, n_states, samples or params");
+    if (c->B == 0 || !c->dN) return fail(c, GPDA_ERR_STATE, "no bursts uploaded");
+    if (b0 < 0 || b1 < b0 || b1 > c->B) return fail(c, GPDA_ERR_ARG, "burst range");
+    if (mode == GPDA_MODE_PHOTON && !c->has_offsets) return fail(c, GPDA_ERR_STATE, "photon mode needs arrival offsets");
+    if ((int64_t)(b1 - b0) * S > (int64_t)INT32_MAX) return fail(c, GPDA_ERR_ARG, "too many units per parameter set");
+    CK(cudaSetDevice(c->device));
+    int rc = prepare_launch(c, mode, P, n, params);
+    if (rc) return rc;
+    return enqueue_range(c, mode, P, n, b0, b1, S, seed, dUnit, c->has_obs, nullptr);
 }
 
 // ---------------------------------------------------------------- expected histogram
@@ -474,6 +492,7 @@ gpda_ctx *gpda_create(int32_t device, const gpda_model *m, int32_t *status) {
     if (bad(cudaSetDevice(device))) return nullptr;
     if (bad(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking))) return nullptr;
     if (bad(cudaEventCreateWithFlags(&c->params_ev, cudaEventDisableTiming))) return nullptr;
+    if (bad(cudaStreamCreateWithFlags(&c->cstream, cudaStreamNonBlocking))) return nullptr;
     if (bad(cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device))) return nullptr;
     if (bad(cudaMalloc(&c->dWork, 2 * sizeof(unsigned int)))) return nullptr;   // work items, CTAs done
     if (bad(cudaMalloc(&c->dLimit, sizeof(unsigned long long)))) return nullptr;
@@ -512,6 +531,8 @@ void gpda_destroy(gpda_ctx *c) {
     if (c->hHist) cudaFreeHost(c->hHist);
     if (c->hChi2) cudaFreeHost(c->hChi2);
     if (c->params_ev) cudaEventDestroy(c->params_ev);
+    for (auto e : c->range_ev) cudaEventDestroy(e);
+    if (c->cstream) { cudaStreamSynchronize(c->cstream); cudaStreamDestroy(c->cstream); }
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -558,7 +579,7 @@ int32_t gpda_upload_bursts(gpda_ctx *c, const int32_t *N, const float *T, const 
     }
     CK(cudaMemsetAsync(c->dFlag, 0, sizeof(unsigned int), c->stream));
     CK(launch_validate(c->dN, c->dT, off_idx ? c->dOffIdx : nullptr, off_idx ? c->dOff : nullptr, B,
-                       c->dFlag, c->num_sms, c->stream));
+                       nph, c->dFlag, c->num_sms, c->stream));
     c->launches += 1;
     CK(cudaMemcpyAsync(c->hFlag, c->dFlag, sizeof(unsigned int), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
@@ -891,6 +912,113 @@ int32_t gpda_autotune(gpda_ctx *c, int32_t mode, int32_t P, int32_t n, const flo
     free_graph(c);               // a captured launch uses the old tile
     c->tuned.push_back({mode, S, best});
     if (tile_out) *tile_out = best;
+    return GPDA_OK;
+}
+
+int32_t gpda_run_host(gpda_ctx *c, int32_t mode, int32_t P, int32_t n, const float *params,
+                      const int32_t *N, const float *T, const int64_t *off_idx, const float *offsets,
+                      int64_t B, int32_t S, uint64_t seed, int32_t ranges, uint64_t *hist_out,
+                      double *chi2_out) {
+    if (!c) return GPDA_ERR_ARG;
+    if (mode != GPDA_MODE_OCCUPANCY && mode != GPDA_MODE_PHOTON) return fail(c, GPDA_ERR_ARG, "mode");
+    if (P < 1 || n < 1 || n > GPDA_MAX_STATES || S < 1 || !params) return fail(c, GPDA_ERR_ARG, "P, n_states, samples or params");
+    if (B < 1 || B > (int64_t)INT32_MAX || !N || !T) return fail(c, GPDA_ERR_ARG, "B, N or T");
+    if ((off_idx == nullptr) != (offsets == nullptr)) return fail(c, GPDA_ERR_ARG, "off_idx and offsets go together");
+    if (mode == GPDA_MODE_PHOTON && !off_idx) return fail(c, GPDA_ERR_ARG, "photon mode needs arrival offsets");
+    if (B * (int64_t)S > (int64_t)INT32_MAX) return fail(c, GPDA_ERR_ARG, "too many units per parameter set");
+    if (ranges < 1 || ranges > 64) return fail(c, GPDA_ERR_ARG, "ranges in [1, 64]");
+    int64_t nph = 0;
+    if (off_idx) {
+        if (off_idx[0] != 0 || off_idx[B] < 0) return fail(c, GPDA_ERR_ARG, "off_idx[0] must be 0 and off_idx[B] >= 0");
+        nph = off_idx[B];
+    }
+    CK(cudaSetDevice(c->device));
+    CK(cudaStreamSynchronize(c->stream));
+    c->B = 0;
+    c->exp_valid = false;
+    free_graph(c);
+    if (B > c->cap_B) {
+        free_dev(c->dN); free_dev(c->dT); free_dev(c->dOffIdx);
+        c->dN = nullptr; c->dT = nullptr; c->dOffIdx = nullptr; c->cap_B = 0;
+        CK(cudaMalloc(&c->dN, sizeof(int32_t) * B));
+        CK(cudaMalloc(&c->dT, sizeof(float) * B));
+        CK(cudaMalloc(&c->dOffIdx, sizeof(int64_t) * (B + 1)));
+        c->cap_B = B;
+    }
+    if (off_idx && nph > c->cap_ph) {
+        free_dev(c->dOff);
+        c->dOff = nullptr; c->cap_ph = 0;
+        CK(cudaMalloc(&c->dOff, sizeof(float) * (nph + kOffPad)));
+        c->cap_ph = nph;
+    }
+    while ((int)c->range_ev.size() < ranges) {
+        cudaEvent_t e;
+        CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        c->range_ev.push_back(e);
+    }
+    c->has_offsets = off_idx != nullptr;
+    c->nph = nph;
+    c->mean_N = (double)nph / (double)B;
+    if (!off_idx) {
+        double sumN = 0.0;
+        for (int64_t b = 0; b < B; ++b) sumN += N[b];
+        c->mean_N = sumN / (double)B;
+    }
+    // the compute stream: parameters, tables, histogram reset; the copy
+    // stream: the flag reset, then each range's copies and validation
+    int rc = prepare_launch(c, mode, P, n, params);
+    if (rc) return rc;
+    CK(cudaMemsetAsync(c->dFlag, 0, sizeof(unsigned int), c->cstream));
+    if (off_idx) CK(cudaMemsetAsync(c->dOff + nph, 0, sizeof(float) * kOffPad, c->cstream));
+    c->B = B;                       // the ranges below address the new store
+    for (int r = 0; r < ranges; ++r) {
+        const int64_t b0 = B * r / ranges, b1 = B * (r + 1) / ranges;
+        if (b1 > b0) {
+            CK(cudaMemcpyAsync(c->dN + b0, N + b0, sizeof(int32_t) * (b1 - b0), cudaMemcpyHostToDevice, c->cstream));
+            CK(cudaMemcpyAsync(c->dT + b0, T + b0, sizeof(float) * (b1 - b0), cudaMemcpyHostToDevice, c->cstream));
+            if (off_idx) {
+                CK(cudaMemcpyAsync(c->dOffIdx + b0, off_idx + b0, sizeof(int64_t) * (b1 - b0 + 1), cudaMemcpyHostToDevice, c->cstream));
+                const int64_t p0 = off_idx[b0], p1 = off_idx[b1];
+                if (p0 >= 0 && p1 > p0 && p1 <= nph)
+                    CK(cudaMemcpyAsync(c->dOff + p0, offsets + p0, sizeof(float) * (p1 - p0), cudaMemcpyHostToDevice, c->cstream));
+                else if (!(p0 >= 0 && p1 >= p0 && p1 <= nph)) {
+                    // host-visible inconsistency: the device check would flag it too
+                    CK(cudaStreamSynchronize(c->cstream));
+                    c->B = 0;
+                    return fail(c, GPDA_ERR_ARG, "burst store rejected: off_idx inconsistent with N;");
+                }
+            }
+            CK(launch_validate(c->dN + b0, c->dT + b0, off_idx ? c->dOffIdx + b0 : nullptr,
+                               off_idx ? c->dOff : nullptr, b1 - b0, nph, c->dFlag, c->num_sms, c->cstream));
+            c->launches += 1;
+        }
+        CK(cudaEventRecord(c->range_ev[r], c->cstream));
+        CK(cudaStreamWaitEvent(c->stream, c->range_ev[r], 0));
+        rc = enqueue_range(c, mode, P, n, b0, b1, S, seed, nullptr, c->has_obs && r == ranges - 1,
+                           c->dFlag);
+        if (rc) { cudaStreamSynchronize(c->stream); c->B = 0; return rc; }
+    }
+    const int nb = c->model.nbins;
+    CK(cudaMemcpyAsync(c->hFlag, c->dFlag, sizeof(unsigned int), cudaMemcpyDeviceToHost, c->stream));
+    if (hist_out) CK(cudaMemcpyAsync(c->hHist, c->dHist, sizeof(unsigned long long) * (size_t)P * nb, cudaMemcpyDeviceToHost, c->stream));
+    if (chi2_out && c->has_obs) CK(cudaMemcpyAsync(c->hChi2, c->dChi2, sizeof(double) * P, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    unsigned f = *c->hFlag;
+    if (f) {
+        c->B = 0;
+        std::string why;
+        if (f & 1u) why += " N outside [0, 2^21];";
+        if (f & 2u) why += " T not finite and >= 0;";
+        if (f & 4u) why += " off_idx inconsistent with N;";
+        if (f & 8u) why += " offset not finite;";
+        if (f & 16u) why += " offsets not sorted within a burst;";
+        return fail(c, GPDA_ERR_ARG, "burst store rejected:" + why);
+    }
+    if (hist_out) std::memcpy(hist_out, c->hHist, sizeof(uint64_t) * (size_t)P * nb);
+    if (chi2_out) {
+        if (c->has_obs) std::memcpy(chi2_out, c->hChi2, sizeof(double) * P);
+        else for (int p = 0; p < P; ++p) chi2_out[p] = NAN;
+    }
     return GPDA_OK;
 }
 

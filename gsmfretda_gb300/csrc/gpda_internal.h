@@ -92,6 +92,8 @@ struct PdaArgs {
     unsigned int *done;           // CTAs finished, zeroed before launch
     int32_t left_pad;
     int32_t n_states;
+    // nonzero *abort_flag (the burst-store validation's): the kernel does nothing
+    const unsigned int *abort_flag;
 };
 
 struct RcArgs {
@@ -121,8 +123,8 @@ cudaError_t launch_rc(const RcArgs &a, cudaStream_t st);
 cudaError_t launch_binom_tables(const DevParams *params, int P, int n_states, float *cdf,
                                 GuideEntry *guide, cudaStream_t st);
 cudaError_t launch_validate(const int32_t *N, const float *T, const int64_t *off_idx,
-                            const float *offsets, int64_t B, unsigned int *flag, int num_sms,
-                            cudaStream_t st);
+                            const float *offsets, int64_t B, int64_t nph, unsigned int *flag,
+                            int num_sms, cudaStream_t st);
 cudaError_t pda_occupancy_blocks(int mode, size_t dyn_smem, int *blocks_per_sm);
 cudaError_t pda_set_smem_limit(int mode, size_t dyn_smem);
 

@@ -271,6 +271,13 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) pda_kernel(const PdaArgs
     __shared__ float s_inv[kInvTable];
     const int tid = threadIdx.x;
     const int lane = tid & 31;
+    // a rejected burst store: nothing to simulate. One read per CTA (the flag
+    // may still change while later ranges are validated), so the whole CTA
+    // takes the same branch.
+    __shared__ int s_abort;
+    if (tid == 0) s_abort = (a.abort_flag && __ldcg(a.abort_flag) != 0u) ? 1 : 0;
+    __syncthreads();
+    if (s_abort) return;
     if (tid < kInvTable) s_inv[tid] = tid > 0 ? 1.0f / (float)tid : 0.0f;
     const unsigned lt_mask = (1u << lane) - 1u;
     int lim = 0;
@@ -717,10 +724,11 @@ binom_table_kernel(const DevParams *params, int P, int n_states, float *cdf_all,
 // ---------------------------------------------------------------- burst-store validation
 
 // One warp per burst: photon counts in range, durations finite and >= 0,
-// off_idx consistent with N, offsets finite and sorted within the burst.
+// off_idx consistent with N and inside [0, nph], offsets finite and sorted
+// within the burst.
 // Sets bits of *flag (1: N, 2: T, 4: off_idx, 8: offset not finite, 16: unsorted).
 __global__ void validate_kernel(const int32_t *N, const float *T, const int64_t *off_idx,
-                                const float *offsets, int64_t B, unsigned int *flag) {
+                                const float *offsets, int64_t B, int64_t nph, unsigned int *flag) {
     const int lane = threadIdx.x & 31;
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -734,8 +742,9 @@ __global__ void validate_kernel(const int32_t *N, const float *T, const int64_t 
         }
         if (off_idx) {
             const int64_t lo = off_idx[b], hi = off_idx[b + 1];
-            if (lane == 0 && hi - lo != (int64_t)nb) bad |= 4u;
-            if (hi - lo == (int64_t)nb && nb > 0) {
+            const bool inside = lo >= 0 && hi <= nph;
+            if (lane == 0 && (hi - lo != (int64_t)nb || !inside)) bad |= 4u;
+            if (hi - lo == (int64_t)nb && nb > 0 && inside) {
                 for (int64_t i = lo + lane; i < hi; i += 32) {
                     const float x = offsets[i];
                     if (!isfinite(x)) bad |= 8u;
@@ -759,12 +768,12 @@ cudaError_t launch_binom_tables(const DevParams *params, int P, int n_states, fl
 }
 
 cudaError_t launch_validate(const int32_t *N, const float *T, const int64_t *off_idx,
-                            const float *offsets, int64_t B, unsigned int *flag, int num_sms,
-                            cudaStream_t st) {
+                            const float *offsets, int64_t B, int64_t nph, unsigned int *flag,
+                            int num_sms, cudaStream_t st) {
     int64_t warps = B;
     int64_t grid = std::min<int64_t>((warps * 32 + 255) / 256, (int64_t)num_sms * 8);
     if (grid < 1) grid = 1;
-    validate_kernel<<<(unsigned)grid, 256, 0, st>>>(N, T, off_idx, offsets, B, flag);
+    validate_kernel<<<(unsigned)grid, 256, 0, st>>>(N, T, off_idx, offsets, B, nph, flag);
     return cudaGetLastError();
 }
 

@@ -64,3 +64,44 @@ def test_autotune_changes_no_result_and_upload_drops_the_graph(gpda_lib):
         eng.upload(bs)
         with pytest.raises(GpdaError):
             eng.graph_run(args, 42)
+
+
+@pytest.mark.parametrize("ranges", [1, 4, 7])
+def test_run_host_equals_upload_and_batched(gpda_lib, ranges):
+    """Upload overlapped with the simulation: same results as uploading first."""
+    bs, n, args, md, S = synth.photon_3state(B=2500, seed=41)
+    rng = np.random.default_rng(42)
+    argsP = np.stack([synth.random_3state_args(rng) for _ in range(2)])
+    with Engine(0, **md) as eng:
+        eng.upload(bs)
+        obs, _ = eng.run_plain(MODE_PHOTON, n, args, 1, 9)
+        eng.set_observed(obs.astype(np.float32))
+        hb, cb = eng.run_batched(MODE_PHOTON, n, argsP, 10, 77)
+        hh, ch = eng.run_host(MODE_PHOTON, n, argsP, 10, 77, bs=bs, ranges=ranges)
+        np.testing.assert_array_equal(hh, hb)
+        np.testing.assert_array_equal(ch, cb)
+        # the store stays uploaded
+        h2, c2 = eng.run_batched(MODE_PHOTON, n, argsP, 10, 77)
+        np.testing.assert_array_equal(h2, hb)
+    bo, no, ao, mo, So = synth.occupancy_2state(B=3000, seed=43)
+    with Engine(0, **mo) as eng:
+        eng.upload(bo)
+        hb, _ = eng.run_batched(MODE_OCCUPANCY, no, ao, So, 5)
+        hh, _ = eng.run_host(MODE_OCCUPANCY, no, ao, So, 5, N=bo.N, T=bo.T, ranges=ranges)
+        np.testing.assert_array_equal(hh, hb)
+
+
+def test_run_host_rejects_a_bad_range(gpda_lib):
+    bs, n, args, md, S = synth.photon_3state(B=2000, seed=44)
+    bad = bs.offsets.copy()
+    i = int(bs.off_idx[1500]) + 3                     # in the last of 4 ranges
+    bad[i], bad[i + 1] = bad[i + 1] + 1e-4, bad[i]
+    with Engine(0, **md) as eng:
+        with pytest.raises(GpdaError):
+            eng.run_host(MODE_PHOTON, n, args, 4, 1, N=bs.N, T=bs.T, off_idx=bs.off_idx,
+                         offsets=bad, ranges=4)
+        with pytest.raises(GpdaError):                # no store is left behind
+            eng.run_plain(MODE_PHOTON, n, args, 4, 1)
+        hh, _ = eng.run_host(MODE_PHOTON, n, args, 4, 1, bs=bs, ranges=4)
+        hp, _ = eng.run_plain(MODE_PHOTON, n, args, 4, 1)
+        np.testing.assert_array_equal(hh[0], hp)
