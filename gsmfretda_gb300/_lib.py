@@ -64,6 +64,7 @@ SIGNATURES = {
     "gpda_autotune": (_I32, [_VP, _I32, _I32, _I32, _VP, _I32, _U64, _VP]),
     "gpda_expected_hist": (_I32, [_VP, _I32, _I32, _VP, _VP, _I32, _U64, _VP, _VP]),
     "gpda_expected_hist_adjoint": (_I32, [_VP, _I32, _I32, _VP, _VP, _I32, _U64, _VP, _VP, _VP]),
+    "gpda_expected_set_tape_limit": (_I32, [_VP, _I64]),
     "gpda_expected_grad": (_I32, [_VP, _I32, _I32, _VP, _VP, _I32, _U64, _VP, _VP, _VP, _VP]),
     "gpda_run_pda_noalloc": (_I32, [C.POINTER(GpdaModel), _I32, _I32, _I32, _VP, _VP, _VP, _VP, _VP,
                                     _I64, _I32, _U64, _VP, _VP, _VP, _VP]),

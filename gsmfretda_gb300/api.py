@@ -194,6 +194,10 @@ class Engine:
                                                    _p(up), _p(dE), _p(dK)), self.ctx)
         return dE, dK
 
+    def expected_tape_limit(self, nbytes):
+        """Device bytes the forward may keep for the adjoint (0: recompute)."""
+        _check(self.lib.gpda_expected_set_tape_limit(self.ctx, int(nbytes)), self.ctx)
+
     def expected_grad(self, n, args, samples, seed, anchor=None):
         """Forward and gradient in one call: hist, chi2, dE, dlnK."""
         a, an, P = self._exp_args(n, args, anchor)

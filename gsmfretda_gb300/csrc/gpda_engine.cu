@@ -76,6 +76,9 @@ struct gpda_ctx {
     double *hExpOut = nullptr;      // pinned: chi2[P], hist[P][nbins], grad[P][16], up[P]
     int cap_exp_out = 0;            // in P
     float *dExpInv = nullptr;
+    float *dTape = nullptr;         // mass tape of the last forward
+    size_t cap_tape = 0;            // bytes
+    int64_t tape_limit = (int64_t)16 << 30;
     bool exp_valid = false;         // the forward state matches exp_key
     std::vector<float> exp_key;
     int exp_P = 0, exp_nblk = 0;
@@ -304,8 +307,19 @@ int exp_prepare(gpda_ctx *c, int P, int n, const float *params, const float *anc
     CK(cudaSetDevice(c->device));
     CK(cudaStreamSynchronize(c->stream));   // pinned staging and scratch are free
     const int nb = c->model.nbins;
+    // the mass tape: per unit 2 nbins floats, when it fits under the limit
+    const int64_t units_p = c->B * (int64_t)S;
+    const double tape_bytes = 4.0 * P * 2.0 * nb * (double)units_p;
+    bool tape = nb <= kExpTapeMaxBins && tape_bytes <= (double)c->tape_limit;
+    if (tape && (size_t)tape_bytes > c->cap_tape) {
+        free_dev(c->dTape);
+        c->dTape = nullptr;
+        c->cap_tape = 0;
+        if (cudaMalloc(&c->dTape, (size_t)tape_bytes) == cudaSuccess) c->cap_tape = (size_t)tape_bytes;
+        else { cudaGetLastError(); c->dTape = nullptr; tape = false; }   // walk the binomial again
+    }
     int nblk = 1, nblk_adj = 1;
-    CK(exp_grid(n, nb, P, c->B * (int64_t)S, c->num_sms, &nblk, &nblk_adj));
+    CK(exp_grid(n, nb, P, units_p, c->num_sms, tape, &nblk, &nblk_adj));
     if (!c->dExpInv) {
         CK(cudaMalloc(&c->dExpInv, sizeof(float) * kExpInvN));
         CK(launch_exp_inv_table(c->dExpInv, c->stream));
@@ -359,6 +373,8 @@ int exp_prepare(gpda_ctx *c, int P, int n, const float *params, const float *anc
     a.gpart = c->dExpGPart;
     a.grad = c->dExpGrad;
     a.dchi2 = nullptr;
+    a.tape = tape ? c->dTape : nullptr;
+    a.units_p = units_p;
     a.limit_hits = c->dLimit;
     a.B = c->B;
     a.S = S;
@@ -522,6 +538,7 @@ void gpda_destroy(gpda_ctx *c) {
     free_dev(c->dExp); free_dev(c->dExpPart); free_dev(c->dExpGPart); free_dev(c->dExpHist);
     free_dev(c->dExpChi2); free_dev(c->dExpGrad); free_dev(c->dExpUp); free_dev(c->dExpG);
     free_dev(c->dExpInv);
+    free_dev(c->dTape);
     if (c->hExp) cudaFreeHost(c->hExp);
     if (c->hExpOut) cudaFreeHost(c->hExpOut);
     if (c->hFlag) cudaFreeHost(c->hFlag);
@@ -1019,6 +1036,14 @@ int32_t gpda_run_host(gpda_ctx *c, int32_t mode, int32_t P, int32_t n, const flo
         if (c->has_obs) std::memcpy(chi2_out, c->hChi2, sizeof(double) * P);
         else for (int p = 0; p < P; ++p) chi2_out[p] = NAN;
     }
+    return GPDA_OK;
+}
+
+int32_t gpda_expected_set_tape_limit(gpda_ctx *c, int64_t bytes) {
+    if (!c) return GPDA_ERR_ARG;
+    if (bytes < 0) return fail(c, GPDA_ERR_ARG, "bytes");
+    c->tape_limit = bytes;
+    c->exp_valid = false;
     return GPDA_OK;
 }
 

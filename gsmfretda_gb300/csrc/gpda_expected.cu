@@ -23,8 +23,10 @@
 //                    fixed order into per-block FP64 partials
 //   exp_chi2_kernel  partials -> expected counts, reduced chi-square (FP64,
 //                    sequential over bins as chi2_kernel) and d chi2 / d count
-//   exp_adj_kernel   re-walks each unit: G = sum g_bin P(x), H = d G / d p,
-//                    and the pathwise (dwells, E) plus score (skeleton) terms
+//   exp_adj_kernel   re-walks each unit's trajectory: G = sum g_bin P(bin),
+//                    H = d G / d p from the mass tape the forward wrote (or by
+//                    walking the binomial again without one), and the pathwise
+//                    (dwells, E) plus score (skeleton) terms
 //   exp_grad_kernel  per-block partials -> gradient, times the upstream d chi2
 // All sums have a fixed order, so results do not depend on scheduling.
 #include <algorithm>
@@ -208,8 +210,10 @@ __device__ __forceinline__ float eps_dp(float e, float g, float ct) {
 }
 
 // Walks the masses of (ba + X) / N, X ~ Binomial(sig, p), one bin at a
-// time, outward from the mode: F(bin, mass, sum of x * mass) is called once
-// per bin touched. Inside a bin the number of terms is known, so the term
+// time, outward from the mode: F(bin, mass, sum of x * mass) is called
+// exactly once for every bin the masses touch (the bin holding the mode is
+// reached from both sides; the downward part of it is held back and joined to
+// the upward part). Inside a bin the number of terms is known, so the term
 // loop carries no bin test; the mass cut is tested every 4 terms.
 template <bool WANT_X, class F>
 __device__ __forceinline__ void binom_bins(int Nb, int sig, int ba, float p, int nbins,
@@ -229,41 +233,8 @@ __device__ __forceinline__ void binom_bins(int Nb, int sig, int ba, float p, int
     const float cut = w0 * kMassCut;
     const float rho = p / q, irho = q / p;
     const bool tab = sig + 1 < kExpInvN;
-    // upward: x = m .. sig, ratio P(x+1)/P(x) = (sig - x) rho / (x + 1)
-    {
-        int x = m;
-        float w = w0;
-        float fs = (float)(sig - m);
-        float fx = (float)m;
-        int b = bin_of(ba + m, Nb, nbins);
-        bool more = true;
-        while (more) {
-            int last = (b < nbins - 1) ? bin_start(b + 1, Nb, nbins) - 1 - ba : sig;
-            if (last > sig) last = sig;
-            int cnt = last - x + 1;
-            float run = 0.0f, runx = 0.0f;
-            while (cnt > 0) {
-                int k = cnt < 4 ? cnt : 4;
-#pragma unroll
-                for (int j = 0; j < 4; ++j) {
-                    if (j < k) {
-                        run += w;
-                        if (WANT_X) runx = fmaf(fx, w, runx);
-                        float iv = tab ? __ldg(inv + x + 1) : 1.0f / (float)(x + 1);
-                        w = w * (fs * rho) * iv;
-                        fs -= 1.0f;
-                        fx += 1.0f;
-                        x += 1;
-                    }
-                }
-                cnt -= k;
-                if (w < cut) { more = false; break; }
-            }
-            flush(b, run, runx);
-            if (x > sig) more = false;
-            ++b;
-        }
-    }
+    const int bm = bin_of(ba + m, Nb, nbins);        // the mode's bin
+    float hold = 0.0f, holdx = 0.0f;                // downward mass inside bin bm
     // downward: x = m-1 .. 0, ratio P(x-1)/P(x) = x / ((sig - x + 1) rho)
     if (m > 0) {
         int x = m - 1;
@@ -293,10 +264,47 @@ __device__ __forceinline__ void binom_bins(int Nb, int sig, int ba, float p, int
                     cnt -= k;
                     if (w < cut) { more = false; break; }
                 }
-                flush(b, run, runx);
+                if (b == bm) { hold = run; holdx = runx; }
+                else flush(b, run, runx);
                 if (x < 0) more = false;
                 --b;
             }
+        }
+    }
+    // upward: x = m .. sig, ratio P(x+1)/P(x) = (sig - x) rho / (x + 1)
+    {
+        int x = m;
+        float w = w0;
+        float fs = (float)(sig - m);
+        float fx = (float)m;
+        int b = bm;
+        bool more = true;
+        while (more) {
+            int last = (b < nbins - 1) ? bin_start(b + 1, Nb, nbins) - 1 - ba : sig;
+            if (last > sig) last = sig;
+            int cnt = last - x + 1;
+            float run = 0.0f, runx = 0.0f;
+            while (cnt > 0) {
+                int k = cnt < 4 ? cnt : 4;
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    if (j < k) {
+                        run += w;
+                        if (WANT_X) runx = fmaf(fx, w, runx);
+                        float iv = tab ? __ldg(inv + x + 1) : 1.0f / (float)(x + 1);
+                        w = w * (fs * rho) * iv;
+                        fs -= 1.0f;
+                        fx += 1.0f;
+                        x += 1;
+                    }
+                }
+                cnt -= k;
+                if (w < cut) { more = false; break; }
+            }
+            if (b == bm) { run += hold; runx += holdx; }
+            flush(b, run, runx);
+            if (x > sig) more = false;
+            ++b;
         }
     }
 }
@@ -311,7 +319,7 @@ __device__ __forceinline__ double warp_sum_fixed(const float *col, int lane) {
     return v;
 }
 
-template <int NS>
+template <int NS, bool TAPE>
 __global__ void __launch_bounds__(kExpThreads) exp_fwd_kernel(const ExpArgs a) {
     extern __shared__ float sh_rows[];          // [nbins][kExpThreads]
     __shared__ float s_inv[kInvTable];
@@ -327,6 +335,7 @@ __global__ void __launch_bounds__(kExpThreads) exp_fwd_kernel(const ExpArgs a) {
     const bool narrow = units + stride <= (int64_t)0xffffffffu;
     int lim = 0;
     float *row = sh_rows + tid;
+    const int nb2 = 2 * a.nbins;
     for (int64_t u = (int64_t)blockIdx.x * kExpThreads + tid; u < units; u += stride) {
         // (32-bit division whenever the unit count allows)
         const int b = narrow ? (int)((uint32_t)u / (uint32_t)a.S) : (int)(u / a.S);
@@ -341,9 +350,25 @@ __global__ void __launch_bounds__(kExpThreads) exp_fwd_kernel(const ExpArgs a) {
         const float eeff = (Tb > 0.0f) ? U.acc / Tb : sP.E[U.sm];
         const float W = expf_(U.lw);
         const float pe = eps_p(eeff, a.gamma, a.ct);
-        binom_bins<false>(Nb, sig, ba, pe, a.nbins, a.inv, [&](int bin, float m, float) {
+        // the unit's tape slots: every touched bin written once (they form one
+        // contiguous range), zeros around them
+        float *t = TAPE ? a.tape + (size_t)p * nb2 * a.units_p + u : nullptr;
+        int bmin = a.nbins, bmax = -1;
+        binom_bins<TAPE>(Nb, sig, ba, pe, a.nbins, a.inv, [&](int bin, float m, float mx) {
             row[bin * kExpThreads] += W * m;
+            if (TAPE) {
+                t[(size_t)bin * a.units_p] = m;
+                t[(size_t)(a.nbins + bin) * a.units_p] = mx;
+                bmin = bin < bmin ? bin : bmin;
+                bmax = bin > bmax ? bin : bmax;
+            }
         });
+        if (TAPE)
+            for (int f = 0; f < a.nbins; ++f)
+                if (f < bmin || f > bmax) {
+                    t[(size_t)f * a.units_p] = 0.0f;
+                    t[(size_t)(a.nbins + f) * a.units_p] = 0.0f;
+                }
     }
     if (lim) atomicAdd(a.limit_hits, (unsigned long long)lim);
     __syncthreads();
@@ -412,7 +437,7 @@ __global__ void __launch_bounds__(256) exp_chi2_kernel(const ExpArgs a) {
     }
 }
 
-template <int NS>
+template <int NS, bool TAPE>
 __global__ void __launch_bounds__(kExpThreads) exp_adj_kernel(const ExpArgs a) {
     constexpr int NG = NS + NS * (NS - 1);
     __shared__ float s_inv[kInvTable];
@@ -448,11 +473,20 @@ __global__ void __launch_bounds__(kExpThreads) exp_adj_kernel(const ExpArgs a) {
         const float W = expf_(U.lw);
         const float pe = eps_p(eeff, a.gamma, a.ct);
         float G = 0.0f, GX = 0.0f;
-        binom_bins<true>(Nb, sig, ba, pe, a.nbins, a.inv, [&](int bin, float m, float mx) {
-            const float gb = s_g[bin];
-            G = fmaf(gb, m, G);
-            GX = fmaf(gb, mx, GX);
-        });
+        if (TAPE) {
+            const float *t = a.tape + (size_t)p * 2 * a.nbins * a.units_p + u;
+            for (int bin = 0; bin < a.nbins; ++bin) {
+                const float gb = s_g[bin];
+                G = fmaf(gb, __ldcs(t + (size_t)bin * a.units_p), G);
+                GX = fmaf(gb, __ldcs(t + (size_t)(a.nbins + bin) * a.units_p), GX);
+            }
+        } else {
+            binom_bins<true>(Nb, sig, ba, pe, a.nbins, a.inv, [&](int bin, float m, float mx) {
+                const float gb = s_g[bin];
+                G = fmaf(gb, m, G);
+                GX = fmaf(gb, mx, GX);
+            });
+        }
         // H = sum g P'(x) = (sum g x P - sig p sum g P) / (p q); zero at p in {0, 1}
         float H = 0.0f;
         if (sig > 0 && pe > 0.0f && pe < 1.0f) H = (GX - (float)sig * pe * G) / (pe * (1.0f - pe));
@@ -518,29 +552,43 @@ __global__ void inv_table_kernel(float *inv) {
     if (k < kExpInvN) inv[k] = k > 0 ? 1.0f / (float)k : 0.0f;
 }
 
+template <int NS, bool TAPE>
+size_t fwd_smem(int nbins) { return sizeof(float) * (size_t)nbins * kExpThreads; }
+
+template <int NS, bool TAPE>
+cudaError_t fwd_t(const ExpArgs &a, cudaStream_t st) {
+    const size_t dyn = fwd_smem<NS, TAPE>(a.nbins);
+    cudaError_t e = cudaFuncSetAttribute(exp_fwd_kernel<NS, TAPE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+    if (e != cudaSuccess) return e;
+    exp_fwd_kernel<NS, TAPE><<<dim3(a.nblk, a.P), kExpThreads, dyn, st>>>(a);
+    return cudaGetLastError();
+}
+
 template <int NS>
 cudaError_t fwd_n(const ExpArgs &a, cudaStream_t st) {
-    const size_t dyn = sizeof(float) * (size_t)a.nbins * kExpThreads;
-    cudaError_t e = cudaFuncSetAttribute(exp_fwd_kernel<NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
-    if (e != cudaSuccess) return e;
-    exp_fwd_kernel<NS><<<dim3(a.nblk, a.P), kExpThreads, dyn, st>>>(a);
-    return cudaGetLastError();
+    return a.tape ? fwd_t<NS, true>(a, st) : fwd_t<NS, false>(a, st);
 }
 
 template <int NS>
 cudaError_t adj_n(const ExpArgs &a, cudaStream_t st) {
-    exp_adj_kernel<NS><<<dim3(a.nblk_adj, a.P), kExpThreads, 0, st>>>(a);
+    if (a.tape) exp_adj_kernel<NS, true><<<dim3(a.nblk_adj, a.P), kExpThreads, 0, st>>>(a);
+    else exp_adj_kernel<NS, false><<<dim3(a.nblk_adj, a.P), kExpThreads, 0, st>>>(a);
     return cudaGetLastError();
 }
 
+template <int NS, bool TAPE>
+cudaError_t occ_t(int nbins, int *fwd, int *adj) {
+    const size_t dyn = fwd_smem<NS, TAPE>(nbins);
+    cudaError_t e = cudaFuncSetAttribute(exp_fwd_kernel<NS, TAPE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+    if (e != cudaSuccess) return e;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(fwd, exp_fwd_kernel<NS, TAPE>, kExpThreads, dyn);
+    if (e != cudaSuccess) return e;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(adj, exp_adj_kernel<NS, TAPE>, kExpThreads, 0);
+}
+
 template <int NS>
-cudaError_t occ_n(int nbins, int *fwd, int *adj) {
-    const size_t dyn = sizeof(float) * (size_t)nbins * kExpThreads;
-    cudaError_t e = cudaFuncSetAttribute(exp_fwd_kernel<NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
-    if (e != cudaSuccess) return e;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(fwd, exp_fwd_kernel<NS>, kExpThreads, dyn);
-    if (e != cudaSuccess) return e;
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(adj, exp_adj_kernel<NS>, kExpThreads, 0);
+cudaError_t occ_n(int nbins, bool tape, int *fwd, int *adj) {
+    return tape ? occ_t<NS, true>(nbins, fwd, adj) : occ_t<NS, false>(nbins, fwd, adj);
 }
 
 }  // namespace
@@ -581,15 +629,15 @@ cudaError_t launch_exp_inv_table(float *inv, cudaStream_t st) {
 // Blocks per parameter set for each kernel: one wave of the device over all
 // parameter sets (the units are strided over the blocks of a set), and no
 // more blocks than the units need.
-cudaError_t exp_grid(int n, int nbins, int P, int64_t units, int num_sms, int *nblk_fwd,
+cudaError_t exp_grid(int n, int nbins, int P, int64_t units, int num_sms, bool tape, int *nblk_fwd,
                      int *nblk_adj) {
     int of = 1, oa = 1;
     cudaError_t e;
     switch (n) {
-    case 1: e = occ_n<1>(nbins, &of, &oa); break;
-    case 2: e = occ_n<2>(nbins, &of, &oa); break;
-    case 3: e = occ_n<3>(nbins, &of, &oa); break;
-    case 4: e = occ_n<4>(nbins, &of, &oa); break;
+    case 1: e = occ_n<1>(nbins, tape, &of, &oa); break;
+    case 2: e = occ_n<2>(nbins, tape, &of, &oa); break;
+    case 3: e = occ_n<3>(nbins, tape, &of, &oa); break;
+    case 4: e = occ_n<4>(nbins, tape, &of, &oa); break;
     default: return cudaErrorInvalidValue;
     }
     if (e != cudaSuccess) return e;

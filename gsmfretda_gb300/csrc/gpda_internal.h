@@ -172,6 +172,11 @@ struct ExpArgs {
     double *gpart;                  // [P][nblk][kExpGrad]
     double *grad;                   // [P][kExpGrad]      [dE(n), dlnK(n(n-1))]
     const double *dchi2;            // [P] upstream gradient, null = 1
+    // mass tape (null: none): per unit, its bin masses P(bin) and the sums
+    // x * P(x) over each bin, [p][2 nbins][units per set]; the forward writes
+    // it and the adjoint reads it instead of walking the binomial again
+    float *tape;
+    int64_t units_p;                // B * S
     unsigned long long *limit_hits;
     int64_t B;
     int32_t S, P, nbins, left_pad, nblk, nblk_adj, n;
@@ -182,8 +187,9 @@ struct ExpArgs {
 cudaError_t launch_exp_forward(const ExpArgs &a, cudaStream_t st);
 cudaError_t launch_exp_adjoint(const ExpArgs &a, cudaStream_t st);
 cudaError_t launch_exp_inv_table(float *inv, cudaStream_t st);
-cudaError_t exp_grid(int n, int nbins, int P, int64_t units, int num_sms, int *nblk_fwd,
+cudaError_t exp_grid(int n, int nbins, int P, int64_t units, int num_sms, bool tape, int *nblk_fwd,
                      int *nblk_adj);
+constexpr int kExpTapeMaxBins = 32;     // the forward's per-unit rows live in shared memory
 int build_exp_params(int n, const float *theta, const float *anchor, float gamma, float ct,
                      ExpParams *out);
 

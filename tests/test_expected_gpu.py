@@ -135,3 +135,21 @@ def test_limits_and_invalid_parameters(gpda_lib):
             eng.expected_hist(n, a, 4, 1)
         with pytest.raises(GpdaError):               # more than 4 states
             eng.expected_hist(5, np.full(30, 100.0, dtype=np.float32), 4, 1)
+
+
+def test_mass_tape_and_recompute_agree(orc, gpda_lib):
+    """The adjoint reads the forward's mass tape, or walks the binomial again
+    when the tape is turned off: the same gradient up to FP32 summation order."""
+    bs, n, truth, md, m, obs, S = _setup(orc, 3, B=3000)
+    th = synth.perturb_args(truth, n, seed=6)
+    with Engine(0, **md) as eng:
+        eng.upload(bs)
+        eng.set_observed(obs)
+        H1, c1, e1, k1 = eng.expected_grad(n, th, S, 4)          # with the tape
+        eng.expected_tape_limit(0)
+        H0, c0, e0, k0 = eng.expected_grad(n, th, S, 4)          # recomputed
+    # (the two forwards differ only in grid size, hence in summation order)
+    np.testing.assert_allclose(H1, H0, rtol=1e-7)
+    np.testing.assert_allclose(c1, c0, rtol=1e-7)
+    g1, g0 = np.concatenate([e1[0], k1[0]]), np.concatenate([e0[0], k0[0]])
+    assert np.abs(g1 - g0).max() <= 1e-5 * np.abs(g0).max()
