@@ -310,7 +310,7 @@ int exp_prepare(gpda_ctx *c, int P, int n, const float *params, const float *anc
     // the mass tape: per unit 2 nbins floats, when it fits under the limit
     const int64_t units_p = c->B * (int64_t)S;
     const double tape_bytes = 4.0 * P * 2.0 * nb * (double)units_p;
-    bool tape = nb <= kExpTapeMaxBins && tape_bytes <= (double)c->tape_limit;
+    bool tape = tape_bytes <= (double)c->tape_limit;
     if (tape && (size_t)tape_bytes > c->cap_tape) {
         free_dev(c->dTape);
         c->dTape = nullptr;

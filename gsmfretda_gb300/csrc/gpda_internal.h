@@ -189,7 +189,6 @@ cudaError_t launch_exp_adjoint(const ExpArgs &a, cudaStream_t st);
 cudaError_t launch_exp_inv_table(float *inv, cudaStream_t st);
 cudaError_t exp_grid(int n, int nbins, int P, int64_t units, int num_sms, bool tape, int *nblk_fwd,
                      int *nblk_adj);
-constexpr int kExpTapeMaxBins = 32;     // the forward's per-unit rows live in shared memory
 int build_exp_params(int n, const float *theta, const float *anchor, float gamma, float ct,
                      ExpParams *out);
 

@@ -215,7 +215,7 @@ int32_t gpda_expected_hist_adjoint(gpda_ctx *ctx, int32_t P, int32_t n_states,
                                    const float *params, const float *anchor, int32_t samples,
                                    uint64_t seed, const double *dchi2, double *dE, double *dlogK);
 /* The forward keeps, per unit, its bin masses and x-weighted bin masses in
- * device memory (4 * P * 2 * nbins * B * samples bytes; nbins <= 32) so that
+ * device memory (4 * P * 2 * nbins * B * samples bytes) so that
  * the adjoint does not walk the binomial again; above `bytes` (default
  * 16 GiB; 0 turns it off) the adjoint recomputes them instead. Same results
  * either way up to FP32 summation order. */
