@@ -16,7 +16,8 @@
 // Binomial masses: the mode's probability by Loader's saddle-point form
 // (C. Loader, "Fast and accurate computation of binomial probabilities",
 // 2000), then the ratio recurrence P(x+1)/P(x) = (sig-x) p / ((x+1) q) in both
-// directions until a mass drops below 2^-30 of the mode's.
+// directions until a mass drops below 2^-24 of the mode's (the neglected tail
+// is below FP32 resolution of the unit's total).
 //
 // Kernels (one parameter set per blockIdx.y, units strided over blockIdx.x):
 //   exp_fwd_kernel   per-thread FP32 bin rows in shared memory, reduced in a
@@ -39,7 +40,7 @@ namespace gpda {
 namespace {
 
 constexpr int kExpThreads = 256;
-constexpr float kMassCut = 0x1p-30f;
+constexpr float kMassCut = 0x1p-24f;
 constexpr uint32_t kExpBgBlock = 0x80000000u;   // above any trajectory block (< 2^15)
 
 // ln(1 - x) for 0 <= x < 1 without forming 1 - x when x is small
@@ -357,8 +358,8 @@ __global__ void __launch_bounds__(kExpThreads) exp_fwd_kernel(const ExpArgs a) {
         binom_bins<TAPE>(Nb, sig, ba, pe, a.nbins, a.inv, [&](int bin, float m, float mx) {
             row[bin * kExpThreads] += W * m;
             if (TAPE) {
-                t[(size_t)bin * a.units_p] = m;
-                t[(size_t)(a.nbins + bin) * a.units_p] = mx;
+                __stcs(t + (size_t)bin * a.units_p, m);
+                __stcs(t + (size_t)(a.nbins + bin) * a.units_p, mx);
                 bmin = bin < bmin ? bin : bmin;
                 bmax = bin > bmax ? bin : bmax;
             }
@@ -366,8 +367,8 @@ __global__ void __launch_bounds__(kExpThreads) exp_fwd_kernel(const ExpArgs a) {
         if (TAPE)
             for (int f = 0; f < a.nbins; ++f)
                 if (f < bmin || f > bmax) {
-                    t[(size_t)f * a.units_p] = 0.0f;
-                    t[(size_t)(a.nbins + f) * a.units_p] = 0.0f;
+                    __stcs(t + (size_t)f * a.units_p, 0.0f);
+                    __stcs(t + (size_t)(a.nbins + f) * a.units_p, 0.0f);
                 }
     }
     if (lim) atomicAdd(a.limit_hits, (unsigned long long)lim);

@@ -216,9 +216,10 @@ int32_t gpda_expected_hist_adjoint(gpda_ctx *ctx, int32_t P, int32_t n_states,
                                    uint64_t seed, const double *dchi2, double *dE, double *dlogK);
 /* The forward keeps, per unit, its bin masses and x-weighted bin masses in
  * device memory (4 * P * 2 * nbins * B * samples bytes) so that
- * the adjoint does not walk the binomial again; above `bytes` (default
- * 16 GiB; 0 turns it off) the adjoint recomputes them instead. Same results
- * either way up to FP32 summation order. */
+ * the adjoint does not walk the binomial again, when the walk is longer than
+ * the 2 nbins values a unit reads back (about 6.5 sqrt(mean N) > 2 nbins);
+ * above `bytes` (default 16 GiB; 0 turns it off) the adjoint recomputes them
+ * instead. Same results either way up to FP32 summation order. */
 int32_t gpda_expected_set_tape_limit(gpda_ctx *ctx, int64_t bytes);
 /* Forward and gradient (dchi2 = 1) in one call, one synchronisation. */
 int32_t gpda_expected_grad(gpda_ctx *ctx, int32_t P, int32_t n_states, const float *params,
