@@ -386,6 +386,8 @@ __global__ void __launch_bounds__(kExpThreads) exp_fwd_kernel(const ExpArgs a) {
 __device__ __forceinline__ double warp_sum_strided(const double *src, int count, size_t stride,
                                                    int lane) {
     double v = 0.0;
+    // (unrolled: the loads go out together, the additions keep their order)
+#pragma unroll 8
     for (int k = lane; k < count; k += 32) v += src[(size_t)k * stride];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
