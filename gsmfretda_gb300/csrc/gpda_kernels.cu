@@ -7,14 +7,20 @@
 //                      simulates (burst, sample) units and bins the proximity
 //                      ratio into a shared-memory histogram with warp-
 //                      aggregated atomics; the histogram is flushed once per
-//                      work item. MODE 0: occupancy-weighted E, one binomial
-//                      split per unit. MODE 1: photon-by-photon state
-//                      assignment, one binomial per dwell segment.
-//   chi2_kernel        reduced chi-square per parameter set in FP64,
-//                      sequential over bins (src/streamWorker.cpp:197-206).
+//                      work item; the last CTA to finish computes the reduced
+//                      chi-square (src/streamWorker.cpp:197-206) in FP64.
+//                      MODE 0: occupancy-weighted E; lanes whose trajectory has
+//                      ended wait until the whole warp runs its background +
+//                      binomial splits together. MODE 1: photon-by-photon
+//                      state assignment, one binomial per dwell segment,
+//                      drawn from tabulated CDFs (one 16-byte guide entry).
+//   binom_table_kernel the photon-mode CDF rows, one warp per row.
+//   chi2_kernel        reduced chi-square per parameter set, for callers that
+//                      launch without an observed histogram in the context.
 //   rc_kernel          mc_kernel's semantics (src/mc.cu:83-197), one thread
 //                      per (burst, sample), fused with the reference's
 //                      histogram binning (src/streamWorker.cpp:33-38).
+//   validate_kernel    burst-store checks, one warp per burst.
 //
 // No tensor cores: nothing here is a contraction. The work is INT32 (Philox)
 // and FP32 ALU bound; HBM traffic is the burst store read once per item.
