@@ -5,7 +5,7 @@
 // the sampled occupancy model's, drawn from the same Philox counters
 // (seed, pword = p, b, s) in the same order (traj_occ in gpda_kernels.cu); it
 // comes from the anchor theta0 and carries the likelihood-ratio weight W (see
-// ExpParams). The background counts are drawn as in final_occ but from counter
+// ExpParams). The background counts are drawn as in the occupancy split but from counter
 // block 2^31 on, so that they do not depend on the trajectory's length. With
 //   E_eff = sum_k dt_k E[s_k] / T,  dt_k = -ln(u_k) / k_exit(s_k; theta)
 //   p     = eps(E_eff) = (g E + ct (1-E)) / (g E + (1+ct)(1-E))

@@ -6,13 +6,6 @@
 namespace gpda {
 
 constexpr int kThreads = 256;       // threads per CTA of the MC kernels
-// occupancy mode: lanes whose trajectory has ended wait until this many can
-// take their background + binomial split together (or no trajectory is left);
-// 32 (every lane) measured fastest: 8 / 16 / 24 / 32 -> 24.5 / 22.6 / 21.6 /
-// 21.4 ms on 64 parameter sets x 50,000 bursts x 50 samples
-#ifndef GPDA_FIN_MIN
-#define GPDA_FIN_MIN 32
-#endif
 #ifndef GPDA_MIN_BLOCKS
 #define GPDA_MIN_BLOCKS 4
 #endif

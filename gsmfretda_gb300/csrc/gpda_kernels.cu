@@ -9,9 +9,9 @@
 //                      aggregated atomics; the histogram is flushed once per
 //                      work item; the last CTA to finish computes the reduced
 //                      chi-square (src/streamWorker.cpp:197-206) in FP64.
-//                      MODE 0: occupancy-weighted E; lanes whose trajectory has
-//                      ended wait until the whole warp runs its background +
-//                      binomial splits together. MODE 1: photon-by-photon
+//                      MODE 0: occupancy-weighted E; rounds of one unit per
+//                      thread: trajectories, then the background + binomial
+//                      splits regrouped by sampler across the CTA. MODE 1: photon-by-photon
 //                      state assignment, one binomial per dwell segment,
 //                      drawn from tabulated CDFs (one 16-byte guide entry).
 //   binom_table_kernel the photon-mode CDF rows, one warp per row.
@@ -152,8 +152,9 @@ __device__ __forceinline__ bool step_pho(Unit &U, const DevParams &P, const floa
 
 // Occupancy mode: one dwell segment per step, draws [state, dwell]; returns
 // true once the trajectory has reached the end of the burst (U.acc then holds
-// the occupancy-weighted efficiency times T). The background and binomial
-// split follow in final_occ.
+// the occupancy-weighted efficiency times T). Then a fresh block for the
+// background and the single binomial split with the occupancy-weighted
+// efficiency (pda_kernel<0>).
 __device__ __forceinline__ bool traj_occ(Unit &U, const DevParams &P, float r0, int &lim) {
     const int st = next_state(U, P, U.r.u01());
     U.st = st;
@@ -198,16 +199,6 @@ __device__ __forceinline__ int background_occ(Rng &r, int navail, float lam_a, f
     return B[0];
 }
 
-// Occupancy mode, after the trajectory: a fresh block for the background and
-// the single binomial split with the occupancy-weighted efficiency.
-__device__ __forceinline__ void final_occ(Unit &U, const DevParams &P, float g, float ct, float bga,
-                                          float bgd, int &lim, const float *inv) {
-    float eeff = (U.Tb > 0.0f) ? U.acc / U.Tb : P.E[U.st];
-    U.r.align();
-    int sig;
-    int ba = background_occ(U.r, U.Nb, bga * U.Tb, bgd * U.Tb, &sig, lim, inv);
-    U.A = binom(U.r, sig, eps_of(eeff, g, ct), lim, inv) + ba;
-}
 
 // warp-aggregated shared-memory histogram increment; all 32 lanes call it
 // (bin < 0: no count)
@@ -275,6 +266,8 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) pda_kernel(const PdaArgs
     __shared__ int s_staged;
     __shared__ int s_next;
     __shared__ float s_inv[kInvTable];
+    __shared__ uint32_t s_ent[10][kThreads];     // occupancy mode: sorted splits
+    __shared__ int s_nf, s_nb;
     const int tid = threadIdx.x;
     const int lane = tid & 31;
     // a rejected burst store: nothing to simulate. One read per CTA (the flag
@@ -329,30 +322,98 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) pda_kernel(const PdaArgs
         const int units = nb * a.S;
         const bool staged = (MODE == 1) && s_staged;
         const uint32_t pw = a.pbase + (uint32_t)p;
+        if (MODE == 0) {
+            // Rounds of kThreads units. 1. each thread runs its unit's
+            // trajectory; 2. background, and the binomial split classified
+            // by sampler (the inversion BINV for n min(p,q) < 10, else BTRD):
+            // its arguments and remaining random words go to a shared list,
+            // BINV from the front, BTRD from the back; 3. thread t finishes
+            // entry t, so at most one warp mixes the two samplers. Every
+            // unit continues its own Philox stream: results do not depend
+            // on which thread finishes it.
+            for (int r0 = 0; r0 < units; r0 += kThreads) {
+                if (tid == 0) { s_nf = 0; s_nb = 0; }
+                const int u = r0 + tid;
+                const bool act = u < units;
+                Unit U;
+                int bin = -1;
+                if (act) {
+                    unit_begin(U, u, a.S, tb0, sN, sT, a.seed, pw);
+                    if (!U.done)
+                        while (!traj_occ(U, sp, a.r0, lim)) {
+                        }
+                }
+                __syncthreads();
+                if (act && !U.done) {
+                    const float eeff = (U.Tb > 0.0f) ? U.acc / U.Tb : sp.E[U.st];
+                    U.r.align();
+                    int sig;
+                    const int ba = background_occ(U.r, U.Nb, a.bg_a * U.Tb, a.bg_d * U.Tb, &sig, lim, s_inv);
+                    const float pe = eps_of(eeff, a.gamma, a.ct);
+                    if (sig <= 0 || !(pe > 0.0f)) U.A = ba;
+                    else if (pe >= 1.0f) U.A = ba + sig;
+                    else {
+                        const float pp = pe > 0.5f ? 1.0f - pe : pe;
+                        const bool inv_sampler = (float)sig * pp < 10.0f;
+                        const int slot = inv_sampler ? atomicAdd(&s_nf, 1) : kThreads - 1 - atomicAdd(&s_nb, 1);
+                        s_ent[0][slot] = (uint32_t)u;
+                        s_ent[1][slot] = (uint32_t)sig;
+                        s_ent[2][slot] = (uint32_t)ba;
+                        s_ent[3][slot] = __float_as_uint(pe);
+                        s_ent[4][slot] = U.r.blk;
+                        s_ent[5][slot] = (uint32_t)U.r.idx;
+                        s_ent[6][slot] = U.r.w0;
+                        s_ent[7][slot] = U.r.w1;
+                        s_ent[8][slot] = U.r.w2;
+                        s_ent[9][slot] = U.r.w3;
+                        U.A = -2;                   // finished in phase 3
+                    }
+                }
+                if (act && U.A != -2) {
+                    const int64_t b = tb0 + U.lb;
+                    if (a.unit_out) a.unit_out[((int64_t)p * (a.b1 - a.b0) + (b - a.b0)) * a.S + U.s] = U.A;
+                    if (U.Nb > 0 && U.A >= 0) {
+                        unsigned v = (unsigned)U.A * (unsigned)a.nbins / (unsigned)U.Nb;
+                        bin = v >= (unsigned)a.nbins ? a.nbins - 1 : (int)v;
+                    }
+                }
+                hist_add_warp(sh, bin);
+                __syncthreads();
+                bin = -1;
+                const int nf = s_nf, nbk = s_nb;
+                if (tid < nf || tid >= kThreads - nbk) {
+                    const int ue = (int)s_ent[0][tid];
+                    const int sig = (int)s_ent[1][tid];
+                    const int ba = (int)s_ent[2][tid];
+                    const float pe = __uint_as_float(s_ent[3][tid]);
+                    const int lb = ue / a.S, ss = ue - lb * a.S;
+                    Rng r;
+                    r.init(a.seed, pw, (uint32_t)(tb0 + lb), (uint32_t)ss);
+                    r.blk = s_ent[4][tid];
+                    r.idx = (int)s_ent[5][tid];
+                    r.w0 = s_ent[6][tid];
+                    r.w1 = s_ent[7][tid];
+                    r.w2 = s_ent[8][tid];
+                    r.w3 = s_ent[9][tid];
+                    const int A = binom(r, sig, pe, lim, s_inv) + ba;
+                    const int64_t b = tb0 + lb;
+                    if (a.unit_out) a.unit_out[((int64_t)p * (a.b1 - a.b0) + (b - a.b0)) * a.S + ss] = A;
+                    const int Nb = sN[lb];
+                    unsigned v = (unsigned)A * (unsigned)a.nbins / (unsigned)Nb;
+                    bin = v >= (unsigned)a.nbins ? a.nbins - 1 : (int)v;
+                }
+                hist_add_warp(sh, bin);
+                __syncthreads();
+            }
+        }
+        // photon mode: one dwell segment per step; a lane whose unit is
+        // finished takes the tile's next unit at once
         Unit U;
-        bool active = tid < units;
-        bool ready = false;     // occupancy mode: trajectory done, split pending
+        bool active = MODE == 1 && tid < units;
         if (active) unit_begin(U, tid, a.S, tb0, sN, sT, a.seed, pw);
         while (__any_sync(0xffffffffu, active)) {
             bool fin = false;
             int bin = -1;
-            if (MODE == 0) {
-                // Trajectory steps are cheap and the background + binomial
-                // split is not: lanes whose trajectory has ended wait, and the
-                // warp runs their splits together once enough are waiting (or
-                // nothing else is left), instead of a few lanes at a time.
-                if (active && !ready) {
-                    if (U.done) fin = true;
-                    else ready = traj_occ(U, sp, a.r0, lim);
-                }
-                const unsigned rmask = __ballot_sync(0xffffffffu, active && ready);
-                const unsigned tmask = __ballot_sync(0xffffffffu, active && !ready && !fin);
-                if (rmask && (__popc(rmask) >= GPDA_FIN_MIN || tmask == 0) && ready) {
-                    final_occ(U, sp, a.gamma, a.ct, a.bg_a, a.bg_d, lim, s_inv);
-                    ready = false;
-                    fin = true;
-                }
-            }
             if (MODE == 1 && active) {
                 fin = U.done;
                 if (!fin) {
