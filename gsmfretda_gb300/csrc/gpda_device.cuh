@@ -165,6 +165,39 @@ __device__ __forceinline__ float cos2pif_(float u) {
     return th * p;
 }
 
+// logf_ for finite normal x > 0 (the uniforms of u01() are in [2^-24, 1]):
+// the same operations without the special cases, so the same bits.
+__device__ __forceinline__ float logf_pos(float x) {
+    uint32_t bits = __float_as_uint(x);
+    int e = (int)(bits >> 23) - 127;
+    float m = __uint_as_float((bits & 0x007FFFFFu) | 0x3F800000u);
+    if (m > kSqrt2) { m = m * 0.5f; e += 1; }
+    float f = m - 1.0f;
+    float s = f / (2.0f + f);
+    float z = s * s;
+    float poly = fmaf(z, fmaf(z, fmaf(z, 0x1.c71c72p-3f, 0x1.24924ap-2f), 0x1.99999ap-2f), 0x1.555556p-1f);
+    float lm = fmaf(s * z, poly, 2.0f * s);
+    float ef = (float)e;
+    return fmaf(ef, kLn2Hi, fmaf(ef, kLn2Lo, lm));
+}
+
+// expf_ for -87 <= x <= 0 (so 2^k with -126 <= k <= 0 is a normal float):
+// the same operations without the range checks, so the same bits.
+__device__ __forceinline__ float expf_neg(float x) {
+    float kf = rintf(x * kLog2e);
+    float r = fmaf(-kf, kLn2Hi, x);
+    r = fmaf(-kf, kLn2Lo, r);
+    float p = 0x1.a01a02p-13f;
+    p = fmaf(p, r, 0x1.6c16c2p-10f);
+    p = fmaf(p, r, 0x1.111112p-7f);
+    p = fmaf(p, r, 0x1.555556p-5f);
+    p = fmaf(p, r, 0x1.555556p-3f);
+    p = fmaf(p, r, 0.5f);
+    p = fmaf(p, r, 1.0f);
+    p = fmaf(p, r, 1.0f);
+    return p * __uint_as_float((uint32_t)((int)kf + 127) << 23);
+}
+
 // Stirling correction fc(k) = ln k! - ((k+1/2) ln(k+1) - (k+1) + ln(2 pi)/2), k < 10
 __device__ __forceinline__ float fc_tab(int k) {
     switch (k) {
@@ -324,7 +357,7 @@ __device__ __forceinline__ int binom_pre(Rng &r, int n, float p, float pp, float
 
 // Poisson by sequential-search inversion, lam < 10.
 __device__ __forceinline__ int pinv(Rng &r, float lam, int &lim, const float *inv) {
-    float L = expf_(-lam);
+    float L = expf_neg(-lam);        // 0 < lam < 10
     // bound = lam + 10 sqrt(lam) + 10 >= 10: evaluated only once k passes 10
     int bound = -1;
     for (int it = 0; it < kMaxRestart; ++it) {

@@ -174,7 +174,7 @@ __device__ __forceinline__ bool exp_walk(const ExpParams &P, Rng &r, int Nb, flo
         st = ns;
         if (!(Tb > 0.0f)) break;
         float u = r.u01();
-        float tau = (P.kexit[st] > 0.0f) ? (-logf_(u)) * P.inv_kexit[st] : kInf;
+        float tau = (P.kexit[st] > 0.0f) ? (-logf_pos(u)) * P.inv_kexit[st] : kInf;
         float tn = t + tau;
         bool cut = seg == kMaxSeg - 1;
         bool last = !(tn < Tb) || cut;

@@ -122,7 +122,7 @@ __device__ __forceinline__ bool step_pho(Unit &U, const DevParams &P, const floa
     const int st = next_state(U, P, U.r.u01());
     U.st = st;
     float u = U.r.u01();
-    float tau = (P.kexit[st] > 0.0f) ? (-logf_(u)) * P.inv_kexit[st] : kInf;
+    float tau = (P.kexit[st] > 0.0f) ? (-logf_pos(u)) * P.inv_kexit[st] : kInf;
     float tn = U.t + tau;
     bool cut = U.seg == kMaxSeg - 1;
     bool last = !(tn < U.Tb) || cut;
@@ -160,7 +160,7 @@ __device__ __forceinline__ bool traj_occ(Unit &U, const DevParams &P, float r0, 
     U.st = st;
     if (!(U.Tb > 0.0f)) return true;
     float u = U.r.u01();
-    float tau = (P.kexit[st] > 0.0f) ? (-logf_(u)) * P.inv_kexit[st] : kInf;
+    float tau = (P.kexit[st] > 0.0f) ? (-logf_pos(u)) * P.inv_kexit[st] : kInf;
     float tn = U.t + tau;
     bool cut = U.seg == kMaxSeg - 1;
     bool last = !(tn < U.Tb) || cut;
