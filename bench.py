@@ -14,7 +14,7 @@ value: device-timed throughput with the burst store resident in HBM (CUDA
 events on the engine stream around each step; a 256 MB write flushes the L2
 between steps, outside the events). e2e: the same metric through the C ABI
 with pinned HOST buffers: each step is one gpda_run_host call, which copies
-the burst store in two ranges (validated on the device) overlapped with the
+the burst store in three ranges of growing size (validated on the device) overlapped with the
 simulation, and reads back histogram + chi-square.
 
 --impl reference times the CPU restatement of the path (the reference has no
@@ -582,7 +582,7 @@ def main():
         t0 = time.perf_counter()
         # one C-ABI call: the store's copy overlapped with the simulation
         h, c2 = eng.run_host(MODE_PHOTON, n, hA, S, 30_000 + k, N=hN, T=hT, off_idx=hOI,
-                             offsets=hOF, ranges=2)
+                             offsets=hOF, ranges=3)
         t1 = time.perf_counter()
         if k >= 2:
             e2e_s.append(t1 - t0)

@@ -309,14 +309,21 @@ __device__ __forceinline__ int btrd(Rng &r, int n, float p, int &lim) {
         v = v * alpha / (a / (us * us) + b);
         float km = fabsf(kf - m);
         if (km <= 15.0f) {
-            float f = 1.0f;
+            // step 3.1: v <= prod (nr/i - rr) over i in (m, k], or v prod
+            // over (k, m] <= 1, with each factor written (nr - rr i) / i and
+            // numerator and denominator scaled by 1/m (both products stay
+            // near 1): two products and one comparison, no division per
+            // factor
             int k = (int)kf, mi = (int)m;
-            if (mi < k) {
-                for (int i = mi + 1; i <= k; ++i) f = f * (nr / (float)i - rr);
-            } else if (mi > k) {
-                for (int i = k + 1; i <= mi; ++i) v = v * (nr / (float)i - rr);
+            int lo = mi < k ? mi : k, hi = mi < k ? k : mi;
+            float im = 1.0f / m;
+            float num = 1.0f, den = 1.0f;
+            for (int i = lo + 1; i <= hi; ++i) {
+                float fi = (float)i;
+                num = num * ((nr - rr * fi) * im);
+                den = den * (fi * im);
             }
-            if (v <= f) return k;
+            if ((mi < k) ? (v * den <= num) : (v * num <= den)) return k;
             continue;
         }
         v = logf_(v);
@@ -364,6 +371,19 @@ __device__ __forceinline__ int pinv(Rng &r, float lam, int &lim, const float *in
         int k = 0;
         float f = L;
         float u = r.u01();
+        // k = 1..10 unrolled with immediate reciprocals (the same values as
+        // inv[k]); the bound is >= 10, so it is first tested at k = 11
+        bool more = u > f;
+#pragma unroll
+        for (int j = 1; j <= 10; ++j) {
+            if (more) {
+                u = u - f;
+                k = j;
+                f = (f * lam) * (1.0f / (float)j);
+                more = u > f;
+            }
+        }
+        if (!more) return k;
         bool over = false;
         while (u > f) {
             u = u - f;

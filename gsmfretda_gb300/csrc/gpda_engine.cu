@@ -993,8 +993,16 @@ int32_t gpda_run_host(gpda_ctx *c, int32_t mode, int32_t P, int32_t n, const flo
     CK(cudaMemsetAsync(c->dFlag, 0, sizeof(unsigned int), c->cstream));
     if (off_idx) CK(cudaMemsetAsync(c->dOff + nph, 0, sizeof(float) * kOffPad, c->cstream));
     c->B = B;                       // the ranges below address the new store
+    // range r ends at burst B (2^(r+1) - 1) / (2^ranges - 1): each range is
+    // twice the one before, so the copy of the next range (the copy engine
+    // moves a burst faster than the kernel simulates it) hides under the
+    // simulation of this one and only the first, smallest copy is exposed
+    auto edge = [&](int r) -> int64_t {
+        if (r >= ranges) return B;
+        return (int64_t)((double)B * (std::ldexp(1.0, r) - 1.0) / (std::ldexp(1.0, ranges) - 1.0));
+    };
     for (int r = 0; r < ranges; ++r) {
-        const int64_t b0 = B * r / ranges, b1 = B * (r + 1) / ranges;
+        const int64_t b0 = edge(r), b1 = edge(r + 1);
         if (b1 > b0) {
             CK(cudaMemcpyAsync(c->dN + b0, N + b0, sizeof(int32_t) * (b1 - b0), cudaMemcpyHostToDevice, c->cstream));
             CK(cudaMemcpyAsync(c->dT + b0, T + b0, sizeof(float) * (b1 - b0), cudaMemcpyHostToDevice, c->cstream));

@@ -154,7 +154,8 @@ int64_t gpda_limit_hits(gpda_ctx *ctx);
 /* Upload and run in one call, the reference-facing path for host data (no
  * reference counterpart: there the copy and the kernel are separate steps).
  * The burst store goes to the device in `ranges` burst ranges (1..64) on a
- * copy stream; each range is validated on the device as gpda_upload_bursts
+ * copy stream, each range twice the size of the one before (range r ends at
+ * burst B (2^(r+1) - 1) / (2^ranges - 1)); each range is validated on the device as gpda_upload_bursts
  * validates, and the Monte-Carlo kernel simulates it as soon as it has
  * arrived, so the copy overlaps the simulation. Every kernel reads the
  * validation flag first and does nothing once a range has been rejected.
