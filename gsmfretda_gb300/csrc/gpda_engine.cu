@@ -168,13 +168,29 @@ int ensure_scratch(gpda_ctx *c, int P) {
     return GPDA_OK;
 }
 
-int tile_bursts(const gpda_ctx *c, int mode, int S) {
+// Bursts per work item for a launch over nb bursts and P parameter sets: the
+// tuned value for (mode, S), else ~2048 units (photon mode: tiles whose
+// offsets fit the shared-memory staging). Occupancy mode then caps it so that
+// the launch has at least 4 work items per resident CTA (a single parameter
+// set otherwise leaves CTAs idle at the end), down to one round of kThreads
+// units. Photon mode keeps its tiles: there a lane takes the tile's next unit
+// as soon as its own is done, and tiles of fewer units per lane measured
+// slower than the end-of-launch imbalance they remove.
+int tile_bursts(const gpda_ctx *c, int mode, int S, int64_t nb, int P) {
+    int tb = 0;
     for (const auto &t : c->tuned)
-        if (t[0] == mode && t[1] == S) return t[2];
-    int tb = (2048 + S - 1) / S;
-    if (mode == GPDA_MODE_PHOTON && c->mean_N > 0.0) {
-        int fit = (int)(0.6 * kSmemCapFloats / c->mean_N);
-        tb = std::min(tb, std::max(fit, 1));
+        if (t[0] == mode && t[1] == S) tb = t[2];
+    if (tb == 0) {
+        tb = (2048 + S - 1) / S;
+        if (mode == GPDA_MODE_PHOTON && c->mean_N > 0.0) {
+            int fit = (int)(0.6 * kSmemCapFloats / c->mean_N);
+            tb = std::min(tb, std::max(fit, 1));
+        }
+    }
+    if (mode == GPDA_MODE_OCCUPANCY) {
+        const int64_t slots = 4 * (int64_t)c->num_sms * std::max(1, c->blocks_per_sm[mode]);
+        const int64_t cap = std::max<int64_t>(nb * (int64_t)std::max(P, 1) / slots, (kThreads + S - 1) / S);
+        if (cap < tb) tb = (int)cap;
     }
     return std::max(1, std::min(tb, kMaxTileBursts));
 }
@@ -248,7 +264,7 @@ int enqueue_range(gpda_ctx *c, int mode, int P, int n, int64_t b0, int64_t b1, i
     a.seed = seed;
     a.P = P;
     a.S = S;
-    a.tile_b = tile_bursts(c, mode, S);
+    a.tile_b = tile_bursts(c, mode, S, b1 - b0, P);
     int64_t ntiles = (b1 - b0 + a.tile_b - 1) / a.tile_b;
     if (ntiles * P > (int64_t)INT32_MAX) return fail(c, GPDA_ERR_ARG, "too many work items");
     a.ntiles = (int)ntiles;
@@ -811,7 +827,7 @@ int32_t gpda_graph_create(gpda_ctx *c, int32_t mode, int32_t P, int32_t n, int32
     a.params = c->dParams; a.hist = c->dHist; a.unit_out = nullptr; a.work = c->dWork;
     a.limit_hits = c->dLimit;
     a.b0 = 0; a.b1 = c->B; a.seed = 0; a.P = P; a.S = S;
-    a.tile_b = tile_bursts(c, mode, S);
+    a.tile_b = tile_bursts(c, mode, S, c->B, P);
     int64_t ntiles = (c->B + a.tile_b - 1) / a.tile_b;
     if (ntiles * P > (int64_t)INT32_MAX) return fail(c, GPDA_ERR_ARG, "too many work items");
     a.ntiles = (int)ntiles; a.n_items = (int)(ntiles * P); a.nbins = nbins;
@@ -909,7 +925,7 @@ int32_t gpda_autotune(gpda_ctx *c, int32_t mode, int32_t P, int32_t n, const flo
     // forget an earlier choice for this shape, then time candidates around the default
     for (size_t i = 0; i < c->tuned.size(); ++i)
         if (c->tuned[i][0] == mode && c->tuned[i][1] == S) { c->tuned.erase(c->tuned.begin() + i); break; }
-    const int base = tile_bursts(c, mode, S);
+    const int base = tile_bursts(c, mode, S, c->B, P);
     std::vector<int> cand;
     for (int f : {-2, -1, 0, 1, 2}) {
         int t = f < 0 ? base >> (-f) : base << f;
