@@ -39,14 +39,18 @@ WORKLOAD = "photon_3state"
 B_FULL = 100_000
 SAMPLES = 100
 HELD_OUT_SEED = 0x0B5E
-# Thread instructions per unit of this workload, from ncu (warp instructions x
-# active threads per instruction / units; profiles/pda_kernel_photon_3state.txt);
-# the fixed cost model (25 per Philox word, 16 per log, 40 per binomial, 2 per
-# photon compare) gives 1,040.
-ALU_OPS_PER_UNIT = 1149.0
+# Algorithmic operations per unit of this workload, by the fixed cost model
+# (25 per 32-bit Philox word, 16 per log, 40 per binomial, 2 per photon
+# compare): D = 4.7 dwell segments per unit (mean exit rate ~2 x 1075 /s over
+# T ~ 1.7 ms) draw 1 + 2D + 4 + D words, D logs and D binomials, and N = 150
+# photons are compared once: (5 + 3D) 25 + 56 D + 2 N = 1,040.
+ALGO_OPS_PER_UNIT = 1040.0
+# Thread instructions the kernel issues per unit, from ncu (warp instructions x
+# active threads per instruction / units; profiles/pda_kernel_photon_3state.txt).
+ISSUED_INST_PER_UNIT = 1246.0
 # DRAM bytes (read + write) of one MC launch on this workload, from the same
 # ncu capture; the algorithmic figure is computed live below.
-NCU_TRAFFIC_BYTES = 69.14e6
+NCU_TRAFFIC_BYTES = 68.58e6
 
 
 def parse():
@@ -596,7 +600,8 @@ def main():
     hbm_peak, peak_kind, sm_max = peaks()
     achieved_gbs = alg_bytes / (kavg_ms * 1e-3) / 1e9
     alu_peak = 152 * 128 * sm_max * 1e6 / 1e9          # FP32/INT32 lane-ops per s, in Gop/s
-    alu_achieved = units / (kavg_ms * 1e-3) * ALU_OPS_PER_UNIT / 1e9
+    alu_achieved = units / (kavg_ms * 1e-3) * ALGO_OPS_PER_UNIT / 1e9
+    alu_issued = units / (kavg_ms * 1e-3) * ISSUED_INST_PER_UNIT / 1e9
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
@@ -614,9 +619,12 @@ def main():
                      "frac": achieved_gbs / hbm_peak,
                      "traffic": NCU_TRAFFIC_BYTES if bs.B == B_FULL else None, "peak_kind": peak_kind,
                      "algorithmic_bytes_per_launch": alg_bytes, "kernel_ms": kavg_ms,
-                     "alu": {"achieved": alu_achieved, "peak": alu_peak, "unit": "Ginst/s",
-                             "frac": alu_achieved / alu_peak, "inst_per_unit": ALU_OPS_PER_UNIT,
-                             "what": "thread-instruction issue rate vs 152 SMs x 128 lanes x SM clock"}},
+                     "alu": {"achieved": alu_achieved, "peak": alu_peak, "unit": "Gop/s",
+                             "frac": alu_achieved / alu_peak, "ops_per_unit": ALGO_OPS_PER_UNIT,
+                             "issued": alu_issued, "issued_frac": alu_issued / alu_peak,
+                             "issued_inst_per_unit": ISSUED_INST_PER_UNIT,
+                             "what": "algorithmic ops (cost model) and issued thread "
+                                     "instructions (ncu) vs 152 SMs x 128 lanes x SM clock"}},
         "chi2_last": float(chi2[0]),
     }
     if rank == 0 and world == 1 and not a.no_cpu_baseline:
