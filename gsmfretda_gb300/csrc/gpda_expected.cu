@@ -387,22 +387,24 @@ __device__ __forceinline__ double warp_sum_strided(const double *src, int count,
                                                    int lane) {
     double v = 0.0;
     // (unrolled: the loads go out together, the additions keep their order)
-#pragma unroll 8
+#pragma unroll 16
     for (int k = lane; k < count; k += 32) v += src[(size_t)k * stride];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
     return v;
 }
 
-// One block of 256 threads per parameter set: a warp per bin sums the
-// per-block partials, then the chi-square (sequential over bins, FP64, as
-// chi2_kernel) and d chi2 / d count for each bin.
-__global__ void __launch_bounds__(256) exp_chi2_kernel(const ExpArgs a) {
+// One block of 1024 threads per parameter set: a warp per bin sums the
+// per-block partials (32 bins at a time: the sums are latency bound), then
+// the chi-square (sequential over bins, FP64, as chi2_kernel) and
+// d chi2 / d count for each bin.
+constexpr int kExpChi2Threads = 1024;
+__global__ void __launch_bounds__(kExpChi2Threads) exp_chi2_kernel(const ExpArgs a) {
     __shared__ double sM[kExpMaxBins];
     __shared__ double s_den;
     const int p = blockIdx.x;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int bin = warp; bin < a.nbins; bin += 8) {
+    for (int bin = warp; bin < a.nbins; bin += kExpChi2Threads / 32) {
         double v = warp_sum_strided(a.part + (size_t)p * a.nblk * a.nbins + bin, a.nblk,
                                     (size_t)a.nbins, lane);
         if (lane == 0) {
@@ -606,7 +608,7 @@ cudaError_t launch_exp_forward(const ExpArgs &a, cudaStream_t st) {
     default: return cudaErrorInvalidValue;
     }
     if (e != cudaSuccess) return e;
-    exp_chi2_kernel<<<a.P, 256, 0, st>>>(a);
+    exp_chi2_kernel<<<a.P, kExpChi2Threads, 0, st>>>(a);
     return cudaGetLastError();
 }
 
