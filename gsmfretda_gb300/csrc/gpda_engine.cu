@@ -29,6 +29,9 @@ struct gpda_ctx {
     cudaStream_t cstream = nullptr;      // copies of gpda_run_host
     cudaEvent_t params_ev = nullptr;
     std::vector<cudaEvent_t> range_ev;   // one per burst range of gpda_run_host
+    std::vector<cudaStream_t> rstream;   // gpda_run_host: the ranges' kernels
+    std::vector<cudaEvent_t> rjoin;      // end of each of those streams
+    cudaEvent_t prep_ev = nullptr;       // gpda_run_host: parameters and tables ready
     gpda_model model{};
     int num_sms = 0;
     // burst store
@@ -104,6 +107,9 @@ struct gpda_ctx {
 namespace {
 
 constexpr int kSmemCapFloats = 8192;  // photon staging: 32 KB of dynamic shared memory
+constexpr int kMaxRanges = 64;        // burst ranges of gpda_run_host
+constexpr int kRangeStreams = 4;      // streams its range kernels are spread over
+constexpr int kFusedCheckSets = 4;    // photon run_host: CTAs check the store up to this P
 constexpr int kOffPad = 8;            // floats of padding behind the offsets array
 
 int fail(gpda_ctx *c, int code, const std::string &msg) {
@@ -240,14 +246,14 @@ int prepare_launch(gpda_ctx *c, int mode, int P, int n, const float *params) {
     return GPDA_OK;
 }
 
-// The Monte-Carlo kernel over bursts [b0, b1) of all P parameter sets, adding
-// into the histogram; with_chi2: the kernel's last CTA also writes the
-// chi-square; abort_flag: see PdaArgs.
-int enqueue_range(gpda_ctx *c, int mode, int P, int n, int64_t b0, int64_t b1, int S,
-                  uint64_t seed, int32_t *dUnit, bool with_chi2, const unsigned int *abort_flag) {
-    CK(cudaMemsetAsync(c->dWork, 0, 2 * sizeof(unsigned int), c->stream));
-    if (b1 == b0) return GPDA_OK;
-    PdaArgs a{};
+// Arguments and grid of the Monte-Carlo kernel over bursts [b0, b1) of all P
+// parameter sets, adding into the histogram; with_chi2: the last CTA also
+// writes the chi-square; abort_flag: see PdaArgs. The caller zeroes *work and
+// *done (c->dWork[0] and [1] unless it sets others).
+int range_args(gpda_ctx *c, int mode, int P, int n, int64_t b0, int64_t b1, int S, uint64_t seed,
+               int32_t *dUnit, bool with_chi2, const unsigned int *abort_flag, PdaArgs &a,
+               int &grid) {
+    a = PdaArgs{};
     a.bcdf = c->dCdf;
     a.bguide = c->dGuide;
     a.N = c->dN;
@@ -285,8 +291,21 @@ int enqueue_range(gpda_ctx *c, int mode, int P, int n, int64_t b0, int64_t b1, i
         a.n_states = n;
     }
     a.abort_flag = abort_flag;
+    grid = (int)std::min<int64_t>(a.n_items, (int64_t)c->num_sms * c->blocks_per_sm[mode]);
+    return GPDA_OK;
+}
+
+// The Monte-Carlo kernel over bursts [b0, b1) on the context stream (see
+// range_args), timed by the context's events.
+int enqueue_range(gpda_ctx *c, int mode, int P, int n, int64_t b0, int64_t b1, int S,
+                  uint64_t seed, int32_t *dUnit, bool with_chi2, const unsigned int *abort_flag) {
+    CK(cudaMemsetAsync(c->dWork, 0, 2 * sizeof(unsigned int), c->stream));
+    if (b1 == b0) return GPDA_OK;
+    PdaArgs a;
+    int grid = 0;
+    int rc = range_args(c, mode, P, n, b0, b1, S, seed, dUnit, with_chi2, abort_flag, a, grid);
+    if (rc) return rc;
     size_t dyn = (mode == GPDA_MODE_PHOTON) ? sizeof(float) * kSmemCapFloats : 0;
-    int grid = std::min<int64_t>(a.n_items, (int64_t)c->num_sms * c->blocks_per_sm[mode]);
     CK(cudaEventRecord(c->k0, c->stream));
     CK(launch_pda(mode, a, grid, dyn, c->stream));
     CK(cudaEventRecord(c->k1, c->stream));
@@ -531,7 +550,8 @@ gpda_ctx *gpda_create(int32_t device, const gpda_model *m, int32_t *status) {
     if (bad(cudaEventCreateWithFlags(&c->params_ev, cudaEventDisableTiming))) return nullptr;
     if (bad(cudaStreamCreateWithFlags(&c->cstream, cudaStreamNonBlocking))) return nullptr;
     if (bad(cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device))) return nullptr;
-    if (bad(cudaMalloc(&c->dWork, 2 * sizeof(unsigned int)))) return nullptr;   // work items, CTAs done
+    // work items, CTAs done, then one work counter per burst range of gpda_run_host
+    if (bad(cudaMalloc(&c->dWork, (2 + kMaxRanges) * sizeof(unsigned int)))) return nullptr;
     if (bad(cudaMalloc(&c->dLimit, sizeof(unsigned long long)))) return nullptr;
     if (bad(cudaMemset(c->dLimit, 0, sizeof(unsigned long long)))) return nullptr;
     if (bad(cudaMalloc(&c->dObs, sizeof(float) * GPDA_MAX_BINS))) return nullptr;
@@ -570,6 +590,9 @@ void gpda_destroy(gpda_ctx *c) {
     if (c->hChi2) cudaFreeHost(c->hChi2);
     if (c->params_ev) cudaEventDestroy(c->params_ev);
     for (auto e : c->range_ev) cudaEventDestroy(e);
+    for (auto e : c->rjoin) cudaEventDestroy(e);
+    for (auto st : c->rstream) { cudaStreamSynchronize(st); cudaStreamDestroy(st); }
+    if (c->prep_ev) cudaEventDestroy(c->prep_ev);
     if (c->cstream) { cudaStreamSynchronize(c->cstream); cudaStreamDestroy(c->cstream); }
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -964,7 +987,7 @@ int32_t gpda_run_host(gpda_ctx *c, int32_t mode, int32_t P, int32_t n, const flo
     if ((off_idx == nullptr) != (offsets == nullptr)) return fail(c, GPDA_ERR_ARG, "off_idx and offsets go together");
     if (mode == GPDA_MODE_PHOTON && !off_idx) return fail(c, GPDA_ERR_ARG, "photon mode needs arrival offsets");
     if (B * (int64_t)S > (int64_t)INT32_MAX) return fail(c, GPDA_ERR_ARG, "too many units per parameter set");
-    if (ranges < 1 || ranges > 64) return fail(c, GPDA_ERR_ARG, "ranges in [1, 64]");
+    if (ranges < 1 || ranges > kMaxRanges) return fail(c, GPDA_ERR_ARG, "ranges in [1, 64]");
     int64_t nph = 0;
     if (off_idx) {
         if (off_idx[0] != 0 || off_idx[B] < 0) return fail(c, GPDA_ERR_ARG, "off_idx[0] must be 0 and off_idx[B] >= 0");
@@ -994,6 +1017,15 @@ int32_t gpda_run_host(gpda_ctx *c, int32_t mode, int32_t P, int32_t n, const flo
         CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         c->range_ev.push_back(e);
     }
+    while ((int)c->rstream.size() < kRangeStreams) {
+        cudaStream_t st;
+        cudaEvent_t e;
+        CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        c->rstream.push_back(st);
+        CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        c->rjoin.push_back(e);
+    }
+    if (!c->prep_ev) CK(cudaEventCreateWithFlags(&c->prep_ev, cudaEventDisableTiming));
     c->has_offsets = off_idx != nullptr;
     c->nph = nph;
     c->mean_N = (double)nph / (double)B;
@@ -1017,6 +1049,41 @@ int32_t gpda_run_host(gpda_ctx *c, int32_t mode, int32_t P, int32_t n, const flo
         if (r >= ranges) return B;
         return (int64_t)((double)B * (std::ldexp(1.0, r) - 1.0) / (std::ldexp(1.0, ranges) - 1.0));
     };
+    // Each range's kernel runs on one of kRangeStreams streams as soon as its
+    // copy is validated, so the last CTAs of one range overlap the first of
+    // the next. Every range has its own work counter; the CTAs-done counter
+    // is shared, and the last CTA of all of them writes the chi-square.
+    // In photon mode with few parameter sets the kernel's CTAs check their
+    // own bursts (PdaArgs::vflag) and no validate_kernel runs: each of those
+    // launches had to wait for SMs held by the previous range's kernel.
+    const bool fused = mode == GPDA_MODE_PHOTON && P <= kFusedCheckSets;
+    const int nr = std::min(ranges, kRangeStreams);
+    std::vector<PdaArgs> ra(ranges);
+    std::vector<int> rgrid(ranges, 0);
+    uint32_t total = 0;
+    for (int r = 0; r < ranges; ++r) {
+        const int64_t b0 = edge(r), b1 = edge(r + 1);
+        if (b1 == b0) continue;
+        rc = range_args(c, mode, P, n, b0, b1, S, seed, nullptr, c->has_obs, c->dFlag, ra[r], rgrid[r]);
+        if (rc) { c->B = 0; return rc; }
+        ra[r].work = c->dWork + 2 + r;
+        if (fused) {
+            ra[r].vflag = c->dFlag;
+            ra[r].nph = nph;
+        }
+        total += (uint32_t)rgrid[r];
+    }
+    for (int r = 0; r < ranges; ++r) ra[r].done_target = total;
+    CK(cudaMemsetAsync(c->dWork, 0, (size_t)(2 + ranges) * sizeof(unsigned int), c->stream));
+    CK(cudaEventRecord(c->prep_ev, c->stream));
+    CK(cudaEventRecord(c->k0, c->stream));
+    auto drain = [&]() {
+        cudaStreamSynchronize(c->cstream);
+        for (int k = 0; k < nr; ++k) cudaStreamSynchronize(c->rstream[k]);
+        cudaStreamSynchronize(c->stream);
+        c->B = 0;
+    };
+    const size_t dyn = (mode == GPDA_MODE_PHOTON) ? sizeof(float) * kSmemCapFloats : 0;
     for (int r = 0; r < ranges; ++r) {
         const int64_t b0 = edge(r), b1 = edge(r + 1);
         if (b1 > b0) {
@@ -1029,21 +1096,34 @@ int32_t gpda_run_host(gpda_ctx *c, int32_t mode, int32_t P, int32_t n, const flo
                     CK(cudaMemcpyAsync(c->dOff + p0, offsets + p0, sizeof(float) * (p1 - p0), cudaMemcpyHostToDevice, c->cstream));
                 else if (!(p0 >= 0 && p1 >= p0 && p1 <= nph)) {
                     // host-visible inconsistency: the device check would flag it too
-                    CK(cudaStreamSynchronize(c->cstream));
-                    c->B = 0;
+                    drain();
                     return fail(c, GPDA_ERR_ARG, "burst store rejected: off_idx inconsistent with N;");
                 }
             }
-            CK(launch_validate(c->dN + b0, c->dT + b0, off_idx ? c->dOffIdx + b0 : nullptr,
-                               off_idx ? c->dOff : nullptr, b1 - b0, nph, c->dFlag, c->num_sms, c->cstream));
-            c->launches += 1;
+            if (!fused) {
+                CK(launch_validate(c->dN + b0, c->dT + b0, off_idx ? c->dOffIdx + b0 : nullptr,
+                                   off_idx ? c->dOff : nullptr, b1 - b0, nph, c->dFlag, c->num_sms, c->cstream));
+                c->launches += 1;
+            }
         }
         CK(cudaEventRecord(c->range_ev[r], c->cstream));
-        CK(cudaStreamWaitEvent(c->stream, c->range_ev[r], 0));
-        rc = enqueue_range(c, mode, P, n, b0, b1, S, seed, nullptr, c->has_obs && r == ranges - 1,
-                           c->dFlag);
-        if (rc) { cudaStreamSynchronize(c->stream); c->B = 0; return rc; }
+        if (rgrid[r] > 0) {
+            cudaStream_t st = c->rstream[r % nr];
+            CK(cudaStreamWaitEvent(st, c->prep_ev, 0));
+            CK(cudaStreamWaitEvent(st, c->range_ev[r], 0));
+            cudaError_t e = launch_pda(mode, ra[r], rgrid[r], dyn, st);
+            if (e != cudaSuccess) { drain(); return fail(c, GPDA_ERR_CUDA, cudaGetErrorString(e)); }
+            c->launches += 1;
+        }
     }
+    for (int k = 0; k < nr; ++k) {
+        CK(cudaEventRecord(c->rjoin[k], c->rstream[k]));
+        CK(cudaStreamWaitEvent(c->stream, c->rjoin[k], 0));
+    }
+    CK(cudaStreamWaitEvent(c->stream, c->range_ev[ranges - 1], 0));
+    CK(cudaEventRecord(c->k1, c->stream));
+    c->timed = true;
+    c->last_chi2 = c->has_obs;
     const int nb = c->model.nbins;
     CK(cudaMemcpyAsync(c->hFlag, c->dFlag, sizeof(unsigned int), cudaMemcpyDeviceToHost, c->stream));
     if (hist_out) CK(cudaMemcpyAsync(c->hHist, c->dHist, sizeof(unsigned long long) * (size_t)P * nb, cudaMemcpyDeviceToHost, c->stream));

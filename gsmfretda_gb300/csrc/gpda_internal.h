@@ -83,10 +83,18 @@ struct PdaArgs {
     const float *obs;             // nbins observed counts
     double *chi2;                 // P
     unsigned int *done;           // CTAs finished, zeroed before launch
+    // CTAs that count into *done: 0 = this launch's grid; launches over burst
+    // ranges that share one counter give the sum of their grids
+    uint32_t done_target;
     int32_t left_pad;
     int32_t n_states;
     // nonzero *abort_flag (the burst-store validation's): the kernel does nothing
     const unsigned int *abort_flag;
+    // photon mode: non-null = every CTA first checks the bursts of its work
+    // item as validate_kernel does (store of nph offsets), ORs the same error
+    // bits into *vflag and skips an item that fails
+    unsigned int *vflag;
+    int64_t nph;
 };
 
 struct RcArgs {

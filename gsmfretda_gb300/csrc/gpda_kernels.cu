@@ -243,7 +243,8 @@ static __device__ __noinline__ void last_cta_chi2(const PdaArgs &a) {
     __shared__ int s_last;
     __threadfence();
     __syncthreads();
-    if (threadIdx.x == 0) s_last = (atomicAdd(a.done, 1u) == gridDim.x - 1) ? 1 : 0;
+    const unsigned target = a.done_target ? a.done_target : gridDim.x;
+    if (threadIdx.x == 0) s_last = (atomicAdd(a.done, 1u) == target - 1) ? 1 : 0;
     __syncthreads();
     if (s_last) {
         __threadfence();
@@ -302,6 +303,21 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) pda_kernel(const PdaArgs
             sT[i] = a.T[tb0 + i];
         }
         for (int i = tid; i < a.nbins; i += kThreads) sh[i] = 0u;
+        if (MODE == 1 && a.vflag) {
+            // the store's checks for the item's bursts (validate_kernel's),
+            // before the reads they bound; offsets follow once staged
+            unsigned bad = 0u;
+            for (int i = tid; i < nb; i += kThreads) {
+                const int32_t n_ = a.N[tb0 + i];
+                const float t_ = a.T[tb0 + i];
+                if (n_ < 0 || n_ > (1 << 21)) bad |= 1u;
+                if (!(t_ >= 0.0f) || !isfinite(t_)) bad |= 2u;
+                const int64_t lo = a.off_idx[tb0 + i], hi = a.off_idx[tb0 + i + 1];
+                if (hi - lo != (int64_t)n_ || lo < 0 || hi > a.nph) bad |= 4u;
+            }
+            if (bad) atomicOr(a.vflag, bad);
+            if (__syncthreads_or(bad != 0u)) continue;
+        }
         if (MODE == 1) {
             // Stage the tile's offsets: copy the 16-byte-aligned span that
             // covers [off_idx[tb0], off_idx[tb0+nb]) (the store is padded).
@@ -322,6 +338,21 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) pda_kernel(const PdaArgs
         const int units = nb * a.S;
         const bool staged = (MODE == 1) && s_staged;
         const uint32_t pw = a.pbase + (uint32_t)p;
+        if (MODE == 1 && a.vflag) {
+            // offsets finite and sorted within each burst; a warp per burst
+            unsigned bad = 0u;
+            for (int i = tid >> 5; i < nb; i += kThreads / 32) {
+                const float *o = staged ? (s_ph + sOff[i]) : (a.offsets + a.off_idx[tb0 + i]);
+                const int n_ = sN[i];
+                for (int j = lane; j < n_; j += 32) {
+                    const float x = o[j];
+                    if (!isfinite(x)) bad |= 8u;
+                    if (j > 0 && x < o[j - 1]) bad |= 16u;
+                }
+            }
+            if (bad) atomicOr(a.vflag, bad);
+            if (__syncthreads_or(bad != 0u)) continue;
+        }
         if (MODE == 0) {
             // Rounds of kThreads units. 1. each thread runs its unit's
             // trajectory; 2. background, and the binomial split classified

@@ -155,13 +155,15 @@ int64_t gpda_limit_hits(gpda_ctx *ctx);
  * reference counterpart: there the copy and the kernel are separate steps).
  * The burst store goes to the device in `ranges` burst ranges (1..64) on a
  * copy stream, each range twice the size of the one before (range r ends at
- * burst B (2^(r+1) - 1) / (2^ranges - 1)); each range is validated on the device as gpda_upload_bursts
- * validates, and the Monte-Carlo kernel simulates it as soon as it has
- * arrived, so the copy overlaps the simulation. Every kernel reads the
- * validation flag first and does nothing once a range has been rejected.
- * Results equal gpda_upload_bursts + gpda_run_batched with the same
- * arguments; the store stays uploaded for later calls. A rejected store
- * returns GPDA_ERR_ARG and leaves no store. */
+ * burst B (2^(r+1) - 1) / (2^ranges - 1)). Each range is validated on the
+ * device as gpda_upload_bursts validates (in photon mode with P <= 4 by the
+ * simulating CTAs themselves, each checking its bursts before reading them),
+ * and its Monte-Carlo kernel starts as soon as it has arrived, on its own
+ * stream, so the copy overlaps the simulation and consecutive ranges'
+ * kernels overlap. Every kernel reads the validation flag first and does
+ * nothing once a range has been rejected. Results equal gpda_upload_bursts +
+ * gpda_run_batched with the same arguments; the store stays uploaded for
+ * later calls. A rejected store returns GPDA_ERR_ARG and leaves no store. */
 int32_t gpda_run_host(gpda_ctx *ctx, int32_t mode, int32_t P, int32_t n_states, const float *params,
                       const int32_t *N, const float *T, const int64_t *off_idx,
                       const float *offsets, int64_t B, int32_t samples, uint64_t seed,

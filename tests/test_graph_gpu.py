@@ -120,3 +120,35 @@ def test_run_host_tiny_store_with_empty_ranges(gpda_lib):
             hh, ch = eng.run_host(MODE_PHOTON, n, a1, 7, 3, bs=bs, ranges=ranges)
             np.testing.assert_array_equal(hh, hb)
             np.testing.assert_array_equal(ch, cb)
+
+
+@pytest.mark.parametrize("P", [1, 6])
+def test_run_host_reports_each_store_error(gpda_lib, P):
+    """The store checks of gpda_run_host (made by the kernel's CTAs for photon
+    mode with few parameter sets, by validate_kernel otherwise) name the
+    same errors as gpda_upload_bursts."""
+    bs, n, args, md, S = synth.photon_3state(B=3000, seed=46)
+    rng = np.random.default_rng(47)
+    argsP = np.stack([synth.random_3state_args(rng) for _ in range(P)])
+    i = int(bs.off_idx[2500]) + 5
+    cases = []
+    T = bs.T.copy()
+    T[1700] = np.nan
+    cases.append((dict(T=T), "T not finite"))
+    off = bs.offsets.copy()
+    off[i] = np.inf
+    cases.append((dict(offsets=off), "offset not finite"))
+    off = bs.offsets.copy()
+    off[i], off[i + 1] = off[i + 1] + 1e-4, off[i]
+    cases.append((dict(offsets=off), "not sorted"))
+    with Engine(0, **md) as eng:
+        for over, why in cases:
+            kw = dict(N=bs.N, T=bs.T, off_idx=bs.off_idx, offsets=bs.offsets)
+            kw.update(over)
+            with pytest.raises(GpdaError, match=why):
+                eng.run_host(MODE_PHOTON, n, argsP, 4, 1, ranges=3, **kw)
+            with pytest.raises(GpdaError, match=why):
+                eng.upload(**kw)
+        hh, _ = eng.run_host(MODE_PHOTON, n, argsP, 4, 1, bs=bs, ranges=3)
+        hb, _ = eng.run_batched(MODE_PHOTON, n, argsP, 4, 1)
+        np.testing.assert_array_equal(hh, hb)
