@@ -1034,13 +1034,6 @@ int32_t gpda_run_host(gpda_ctx *c, int32_t mode, int32_t P, int32_t n, const flo
         for (int64_t b = 0; b < B; ++b) sumN += N[b];
         c->mean_N = sumN / (double)B;
     }
-    // the compute stream: parameters, tables, histogram reset; the copy
-    // stream: the flag reset, then each range's copies and validation
-    int rc = prepare_launch(c, mode, P, n, params);
-    if (rc) return rc;
-    CK(cudaMemsetAsync(c->dFlag, 0, sizeof(unsigned int), c->cstream));
-    if (off_idx) CK(cudaMemsetAsync(c->dOff + nph, 0, sizeof(float) * kOffPad, c->cstream));
-    c->B = B;                       // the ranges below address the new store
     // range r ends at burst B (2^(r+1) - 1) / (2^ranges - 1): each range is
     // twice the one before, so the copy of the next range (the copy engine
     // moves a burst faster than the kernel simulates it) hides under the
@@ -1049,41 +1042,23 @@ int32_t gpda_run_host(gpda_ctx *c, int32_t mode, int32_t P, int32_t n, const flo
         if (r >= ranges) return B;
         return (int64_t)((double)B * (std::ldexp(1.0, r) - 1.0) / (std::ldexp(1.0, ranges) - 1.0));
     };
-    // Each range's kernel runs on one of kRangeStreams streams as soon as its
-    // copy is validated, so the last CTAs of one range overlap the first of
-    // the next. Every range has its own work counter; the CTAs-done counter
-    // is shared, and the last CTA of all of them writes the chi-square.
     // In photon mode with few parameter sets the kernel's CTAs check their
     // own bursts (PdaArgs::vflag) and no validate_kernel runs: each of those
     // launches had to wait for SMs held by the previous range's kernel.
     const bool fused = mode == GPDA_MODE_PHOTON && P <= kFusedCheckSets;
     const int nr = std::min(ranges, kRangeStreams);
-    std::vector<PdaArgs> ra(ranges);
-    std::vector<int> rgrid(ranges, 0);
-    uint32_t total = 0;
-    for (int r = 0; r < ranges; ++r) {
-        const int64_t b0 = edge(r), b1 = edge(r + 1);
-        if (b1 == b0) continue;
-        rc = range_args(c, mode, P, n, b0, b1, S, seed, nullptr, c->has_obs, c->dFlag, ra[r], rgrid[r]);
-        if (rc) { c->B = 0; return rc; }
-        ra[r].work = c->dWork + 2 + r;
-        if (fused) {
-            ra[r].vflag = c->dFlag;
-            ra[r].nph = nph;
-        }
-        total += (uint32_t)rgrid[r];
-    }
-    for (int r = 0; r < ranges; ++r) ra[r].done_target = total;
-    CK(cudaMemsetAsync(c->dWork, 0, (size_t)(2 + ranges) * sizeof(unsigned int), c->stream));
-    CK(cudaEventRecord(c->prep_ev, c->stream));
-    CK(cudaEventRecord(c->k0, c->stream));
     auto drain = [&]() {
         cudaStreamSynchronize(c->cstream);
         for (int k = 0; k < nr; ++k) cudaStreamSynchronize(c->rstream[k]);
         cudaStreamSynchronize(c->stream);
         c->B = 0;
     };
-    const size_t dyn = (mode == GPDA_MODE_PHOTON) ? sizeof(float) * kSmemCapFloats : 0;
+    // The copy stream first (the host prepares the parameters while the
+    // first range is in flight): the flag reset, then each range's copies
+    // (and validation), each range closed by its event.
+    CK(cudaMemsetAsync(c->dFlag, 0, sizeof(unsigned int), c->cstream));
+    if (off_idx) CK(cudaMemsetAsync(c->dOff + nph, 0, sizeof(float) * kOffPad, c->cstream));
+    c->B = B;                       // the ranges below address the new store
     for (int r = 0; r < ranges; ++r) {
         const int64_t b0 = edge(r), b1 = edge(r + 1);
         if (b1 > b0) {
@@ -1107,14 +1082,42 @@ int32_t gpda_run_host(gpda_ctx *c, int32_t mode, int32_t P, int32_t n, const flo
             }
         }
         CK(cudaEventRecord(c->range_ev[r], c->cstream));
-        if (rgrid[r] > 0) {
-            cudaStream_t st = c->rstream[r % nr];
-            CK(cudaStreamWaitEvent(st, c->prep_ev, 0));
-            CK(cudaStreamWaitEvent(st, c->range_ev[r], 0));
-            cudaError_t e = launch_pda(mode, ra[r], rgrid[r], dyn, st);
-            if (e != cudaSuccess) { drain(); return fail(c, GPDA_ERR_CUDA, cudaGetErrorString(e)); }
-            c->launches += 1;
+    }
+    // The compute stream: parameters, tables, histogram and counter resets.
+    // Each range's kernel then runs on one of kRangeStreams streams as soon
+    // as its copy is in, so the last CTAs of one range overlap the first of
+    // the next. Every range has its own work counter; the CTAs-done counter
+    // is shared, and the last CTA of all of them writes the chi-square.
+    int rc = prepare_launch(c, mode, P, n, params);
+    if (rc) { drain(); return rc; }
+    std::vector<PdaArgs> ra(ranges);
+    std::vector<int> rgrid(ranges, 0);
+    uint32_t total = 0;
+    for (int r = 0; r < ranges; ++r) {
+        const int64_t b0 = edge(r), b1 = edge(r + 1);
+        if (b1 == b0) continue;
+        rc = range_args(c, mode, P, n, b0, b1, S, seed, nullptr, c->has_obs, c->dFlag, ra[r], rgrid[r]);
+        if (rc) { drain(); return rc; }
+        ra[r].work = c->dWork + 2 + r;
+        if (fused) {
+            ra[r].vflag = c->dFlag;
+            ra[r].nph = nph;
         }
+        total += (uint32_t)rgrid[r];
+    }
+    for (int r = 0; r < ranges; ++r) ra[r].done_target = total;
+    CK(cudaMemsetAsync(c->dWork, 0, (size_t)(2 + ranges) * sizeof(unsigned int), c->stream));
+    CK(cudaEventRecord(c->prep_ev, c->stream));
+    CK(cudaEventRecord(c->k0, c->stream));
+    const size_t dyn = (mode == GPDA_MODE_PHOTON) ? sizeof(float) * kSmemCapFloats : 0;
+    for (int r = 0; r < ranges; ++r) {
+        if (rgrid[r] == 0) continue;
+        cudaStream_t st = c->rstream[r % nr];
+        CK(cudaStreamWaitEvent(st, c->prep_ev, 0));
+        CK(cudaStreamWaitEvent(st, c->range_ev[r], 0));
+        cudaError_t e = launch_pda(mode, ra[r], rgrid[r], dyn, st);
+        if (e != cudaSuccess) { drain(); return fail(c, GPDA_ERR_CUDA, cudaGetErrorString(e)); }
+        c->launches += 1;
     }
     for (int k = 0; k < nr; ++k) {
         CK(cudaEventRecord(c->rjoin[k], c->rstream[k]));
