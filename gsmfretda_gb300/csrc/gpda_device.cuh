@@ -362,8 +362,11 @@ __device__ __forceinline__ int binom_pre(Rng &r, int n, float p, float pp, float
     return flip ? n - x : x;
 }
 
-// Poisson by sequential-search inversion, lam < 10.
-__device__ __forceinline__ int pinv(Rng &r, float lam, int &lim, const float *inv) {
+// Poisson by sequential-search inversion, lam < 10. RES: also the residual
+// of the accepted uniform inside the drawn count's interval,
+// res = (u - F(k-1)) / P(k), uniform on (0, 1] given k.
+template <bool RES>
+__device__ __forceinline__ int pinv_t(Rng &r, float lam, int &lim, const float *inv, float &res) {
     float L = expf_neg(-lam);        // 0 < lam < 10
     // bound = lam + 10 sqrt(lam) + 10 >= 10: evaluated only once k passes 10
     int bound = -1;
@@ -383,21 +386,29 @@ __device__ __forceinline__ int pinv(Rng &r, float lam, int &lim, const float *in
                 more = u > f;
             }
         }
-        if (!more) return k;
         bool over = false;
-        while (u > f) {
-            u = u - f;
-            k += 1;
-            if (k > 10) {
+        if (more) {
+            while (u > f) {
+                u = u - f;
+                k += 1;
                 if (bound < 0) bound = (int)(lam + 10.0f * sqrtf(lam) + 10.0f);
                 if (k > bound) { over = true; break; }
+                f = (f * lam) * inv[k];
             }
-            f = (f * lam) * inv[k];
         }
-        if (!over) return k;
+        if (!over) {
+            if (RES) res = u / f;
+            return k;
+        }
     }
     lim += 1;
+    if (RES) res = 0.5f;
     return (int)lam;
+}
+
+__device__ __forceinline__ int pinv(Rng &r, float lam, int &lim, const float *inv) {
+    float unused;
+    return pinv_t<false>(r, lam, lim, inv, unused);
 }
 
 __device__ __forceinline__ float logfact(float k) {
@@ -500,6 +511,42 @@ __device__ __forceinline__ int background(Rng &r, int navail, float lam_a, float
     }
     *sig = avail;
     return B[0];
+}
+
+// Background of one photon-mode segment as a pair: T = A + D ~ Poisson(lam),
+// lam = (bg_a + bg_d) dt, split by A ~ Binomial(T, pa), pa = bg_a / (bg_a +
+// bg_d), which has the law of independent Poisson(bg_a dt) and
+// Poisson(bg_d dt). For lam < 10, T comes from one uniform by inversion and
+// the split from T Bernoulli trials on that uniform's residual (uniform on
+// (0, 1] given T), rescaled after each trial: one random word in all for the
+// pair. bgc = {bg_a + bg_d, pa, 1 / pa, 1 / (1 - pa)}. Clipping to the
+// segment's photons as background().
+__device__ __forceinline__ int background_pair(Rng &r, int navail, float dt, const float *bgc, int *sig,
+                                               int &lim, const float *inv) {
+    const float lam = bgc[0] * dt;
+    int T = 0, A = 0;
+    if (lam > 0.0f) {
+        if (lam < 10.0f) {
+            const float pa = bgc[1], ipa = bgc[2], iqa = bgc[3];
+            float res;
+            T = pinv_t<true>(r, lam, lim, inv, res);
+            for (int i = 0; i < T; ++i) {
+                if (res <= pa) { A += 1; res = res * ipa; }
+                else res = (res - pa) * iqa;
+            }
+        } else {
+            T = ptrs(r, lam, lim);
+            A = binom(r, T, bgc[1], lim, inv);
+        }
+    }
+    int D = T - A;
+    int avail = navail;
+    if (A > avail) A = (int)floorf((float)avail * r.u01());
+    avail -= A;
+    if (D > avail) D = (int)floorf((float)avail * r.u01());
+    avail -= D;
+    *sig = avail;
+    return A;
 }
 
 }  // namespace gpda

@@ -110,12 +110,13 @@ __device__ __forceinline__ int binom_table(Rng &r, int n, const DevParams &P, in
 }
 
 // Photon mode: one dwell segment. Draw order per step: a fresh Philox block
-// [state, dwell, background A, background D], then (if the segment holds
-// photons) a fresh block for the binomial. Photons whose arrival offset falls
-// in the segment take its state; Poisson background, then Binomial(signal,
-// eps_state).
+// [state, dwell, background pair, binomial] (a rare extra draw of the
+// background or the samplers continues in the following blocks). Photons
+// whose arrival offset falls in the segment take its state; the Poisson
+// background pair (background_pair, bgc its constants), then
+// Binomial(signal, eps_state).
 __device__ __forceinline__ bool step_pho(Unit &U, const DevParams &P, const float *offs, float g,
-                                         float ct, float r0, float bga, float bgd, int &lim,
+                                         float ct, float r0, const float *bgc, int &lim,
                                          const float *inv, const float *cdf_p,
                                          const GuideEntry *guide_p) {
     U.r.align_now();   // the state draw follows at once
@@ -134,8 +135,7 @@ __device__ __forceinline__ bool step_pho(Unit &U, const DevParams &P, const floa
     int nk = hi - U.lo;
     if (nk > 0) {
         int sig;
-        int ba = background(U.r, nk, bga * dt, bgd * dt, &sig, lim, inv);
-        U.r.align();
+        int ba = background_pair(U.r, nk, dt, bgc, &sig, lim, inv);
         if (P.V[st] > 0.0f) {
             float ek = eps_of(broaden(U.r, P.E[st], r0, P.V[st]), g, ct);
             U.A += binom(U.r, sig, ek, lim, inv) + ba;
@@ -279,6 +279,16 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) pda_kernel(const PdaArgs
     __syncthreads();
     if (s_abort) return;
     if (tid < kInvTable) s_inv[tid] = tid > 0 ? 1.0f / (float)tid : 0.0f;
+    // photon mode: the background pair's constants (background_pair)
+    __shared__ float s_bgc[4];
+    if (MODE == 1 && tid == 0) {
+        const float bgs = a.bg_a + a.bg_d;
+        const float pa = a.bg_a / bgs;
+        s_bgc[0] = bgs;
+        s_bgc[1] = pa;
+        s_bgc[2] = 1.0f / pa;
+        s_bgc[3] = 1.0f / (1.0f - pa);
+    }
     const unsigned lt_mask = (1u << lane) - 1u;
     int lim = 0;
     for (;;) {
@@ -449,7 +459,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) pda_kernel(const PdaArgs
                 fin = U.done;
                 if (!fin) {
                     const float *offs = staged ? (s_ph + sOff[U.lb]) : (a.offsets + a.off_idx[tb0 + U.lb]);
-                    fin = step_pho(U, sp, offs, a.gamma, a.ct, a.r0, a.bg_a, a.bg_d, lim, s_inv,
+                    fin = step_pho(U, sp, offs, a.gamma, a.ct, a.r0, s_bgc, lim, s_inv,
                                    a.bcdf + (size_t)p * sp.n * kTableRows,
                                    a.bguide + (size_t)p * sp.n * kTableRows);
                 }
