@@ -110,6 +110,7 @@ constexpr int kSmemCapFloats = 8192;  // photon staging: 32 KB of dynamic shared
 constexpr int kMaxRanges = 64;        // burst ranges of gpda_run_host
 constexpr int kRangeStreams = 4;      // streams its range kernels are spread over
 constexpr int kFusedCheckSets = 4;    // photon run_host: CTAs check the store up to this P
+constexpr double kRangeGrowth = 1.5;  // run_host: each burst range 1.5 x the one before
 constexpr int kOffPad = 8;            // floats of padding behind the offsets array
 
 int fail(gpda_ctx *c, int code, const std::string &msg) {
@@ -1034,13 +1035,15 @@ int32_t gpda_run_host(gpda_ctx *c, int32_t mode, int32_t P, int32_t n, const flo
         for (int64_t b = 0; b < B; ++b) sumN += N[b];
         c->mean_N = sumN / (double)B;
     }
-    // range r ends at burst B (2^(r+1) - 1) / (2^ranges - 1): each range is
-    // twice the one before, so the copy of the next range (the copy engine
-    // moves a burst faster than the kernel simulates it) hides under the
-    // simulation of this one and only the first, smallest copy is exposed
+    // range r ends at burst B (g^r - 1) / (g^ranges - 1), g = kRangeGrowth:
+    // each range is g times the one before, so the copy of the next range
+    // (the copy engine moves a burst about twice as fast as the kernel
+    // simulates it) hides under the simulation of this one and only the
+    // first, smallest copy is exposed
     auto edge = [&](int r) -> int64_t {
         if (r >= ranges) return B;
-        return (int64_t)((double)B * (std::ldexp(1.0, r) - 1.0) / (std::ldexp(1.0, ranges) - 1.0));
+        return (int64_t)((double)B * (std::pow(kRangeGrowth, r) - 1.0) /
+                         (std::pow(kRangeGrowth, ranges) - 1.0));
     };
     // In photon mode with few parameter sets the kernel's CTAs check their
     // own bursts (PdaArgs::vflag) and no validate_kernel runs: each of those

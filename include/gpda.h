@@ -154,8 +154,8 @@ int64_t gpda_limit_hits(gpda_ctx *ctx);
 /* Upload and run in one call, the reference-facing path for host data (no
  * reference counterpart: there the copy and the kernel are separate steps).
  * The burst store goes to the device in `ranges` burst ranges (1..64) on a
- * copy stream, each range twice the size of the one before (range r ends at
- * burst B (2^(r+1) - 1) / (2^ranges - 1)). Each range is validated on the
+ * copy stream, each range 1.5 times the size of the one before (range r ends
+ * at burst B (1.5^(r+1) - 1) / (1.5^ranges - 1)). Each range is validated on the
  * device as gpda_upload_bursts validates (in photon mode with P <= 4 by the
  * simulating CTAs themselves, each checking its bursts before reading them),
  * and its Monte-Carlo kernel starts as soon as it has arrived, on its own
