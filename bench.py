@@ -47,10 +47,10 @@ HELD_OUT_SEED = 0x0B5E
 ALGO_OPS_PER_UNIT = 1040.0
 # Thread instructions the kernel issues per unit, from ncu (warp instructions x
 # active threads per instruction / units; profiles/pda_kernel_photon_3state.txt).
-ISSUED_INST_PER_UNIT = 1246.0
+ISSUED_INST_PER_UNIT = 1016.0
 # DRAM bytes (read + write) of one MC launch on this workload, from the same
 # ncu capture; the algorithmic figure is computed live below.
-NCU_TRAFFIC_BYTES = 68.58e6
+NCU_TRAFFIC_BYTES = 68.64e6
 
 
 def parse():
