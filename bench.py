@@ -13,9 +13,10 @@ samples per burst, fused 21-bin histogram + FP64 reduced chi-square.
 value: device-timed throughput with the burst store resident in HBM (CUDA
 events on the engine stream around each step; a 256 MB write flushes the L2
 between steps, outside the events). e2e: the same metric through the C ABI
-with pinned HOST buffers: each step is one gpda_run_host call, which copies
-the burst store in three ranges of growing size (validated on the device) overlapped with the
-simulation, and reads back histogram + chi-square.
+with pinned HOST buffers: each step is one gpda_run_host call, whose kernel
+reads the 61.5 MB burst store from the pinned host arrays over the host link
+(each CTA checks its bursts, stages them and writes them through to the
+device store), and reads back histogram + chi-square.
 
 --impl reference times the CPU restatement of the path (the reference has no
 CPU Monte-Carlo of its own) on the host cores of this machine, all threads.
@@ -584,7 +585,8 @@ def main():
         l2_flush()
         eng.synchronize()
         t0 = time.perf_counter()
-        # one C-ABI call: the store's copy overlapped with the simulation
+        # one C-ABI call: the kernel reads the pinned store in place (the
+        # copy path in burst ranges serves pageable arrays)
         h, c2 = eng.run_host(MODE_PHOTON, n, hA, S, 30_000 + k, N=hN, T=hT, off_idx=hOI,
                              offsets=hOF, ranges=3)
         t1 = time.perf_counter()

@@ -100,7 +100,7 @@ struct gpda_ctx {
     int last_P = 0;
     bool last_chi2 = false;
     int64_t launches = 0;
-    int blocks_per_sm[2] = {0, 0};
+    int blocks_per_sm[3] = {0, 0, 0};   // resident CTAs per SM by launch mode
     std::string err;
 };
 
@@ -313,6 +313,50 @@ int enqueue_range(gpda_ctx *c, int mode, int P, int n, int64_t b0, int64_t b1, i
     c->timed = true;
     c->launches += 1;
     c->last_chi2 = with_chi2;
+    return GPDA_OK;
+}
+
+// The device address of a host array [p, p + bytes) in page-locked memory
+// (cudaHostAlloc, cudaMallocHost, cudaHostRegister), checked at both ends;
+// null for any other memory.
+const void *mapped_host(const void *p, size_t bytes) {
+    if (!p || bytes == 0) return nullptr;
+    cudaPointerAttributes a0{}, a1{};
+    if (cudaPointerGetAttributes(&a0, p) != cudaSuccess) { cudaGetLastError(); return nullptr; }
+    const char *q = static_cast<const char *>(p) + (bytes - 1);
+    if (cudaPointerGetAttributes(&a1, q) != cudaSuccess) { cudaGetLastError(); return nullptr; }
+    if (a0.type != cudaMemoryTypeHost || a1.type != cudaMemoryTypeHost || !a0.devicePointer || !a1.devicePointer)
+        return nullptr;
+    if (static_cast<const char *>(a1.devicePointer) - static_cast<const char *>(a0.devicePointer) !=
+        (ptrdiff_t)(bytes - 1))
+        return nullptr;
+    return a0.devicePointer;
+}
+
+// End of a gpda_run_host call: the store's check flag, histogram and
+// chi-square to the host (one synchronisation), then the flag's verdict.
+int host_run_results(gpda_ctx *c, int P, uint64_t *hist_out, double *chi2_out) {
+    const int nb = c->model.nbins;
+    CK(cudaMemcpyAsync(c->hFlag, c->dFlag, sizeof(unsigned int), cudaMemcpyDeviceToHost, c->stream));
+    if (hist_out) CK(cudaMemcpyAsync(c->hHist, c->dHist, sizeof(unsigned long long) * (size_t)P * nb, cudaMemcpyDeviceToHost, c->stream));
+    if (chi2_out && c->has_obs) CK(cudaMemcpyAsync(c->hChi2, c->dChi2, sizeof(double) * P, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    unsigned f = *c->hFlag;
+    if (f) {
+        c->B = 0;
+        std::string why;
+        if (f & 1u) why += " N outside [0, 2^21];";
+        if (f & 2u) why += " T not finite and >= 0;";
+        if (f & 4u) why += " off_idx inconsistent with N;";
+        if (f & 8u) why += " offset not finite;";
+        if (f & 16u) why += " offsets not sorted within a burst;";
+        return fail(c, GPDA_ERR_ARG, "burst store rejected:" + why);
+    }
+    if (hist_out) std::memcpy(hist_out, c->hHist, sizeof(uint64_t) * (size_t)P * nb);
+    if (chi2_out) {
+        if (c->has_obs) std::memcpy(chi2_out, c->hChi2, sizeof(double) * P);
+        else for (int p = 0; p < P; ++p) chi2_out[p] = NAN;
+    }
     return GPDA_OK;
 }
 
@@ -563,7 +607,9 @@ gpda_ctx *gpda_create(int32_t device, const gpda_model *m, int32_t *status) {
     if (bad(cudaEventRecord(c->params_ev, c->stream))) return nullptr;
     if (bad(pda_occupancy_blocks(0, 0, &c->blocks_per_sm[0]))) return nullptr;
     if (bad(pda_occupancy_blocks(1, sizeof(float) * kSmemCapFloats, &c->blocks_per_sm[1]))) return nullptr;
-    for (int i = 0; i < 2; ++i) c->blocks_per_sm[i] = std::max(1, c->blocks_per_sm[i]);
+    if (bad(pda_occupancy_blocks(kModePhotonDirect, sizeof(float) * kSmemCapFloats,
+                                 &c->blocks_per_sm[kModePhotonDirect]))) return nullptr;
+    for (int i = 0; i < 3; ++i) c->blocks_per_sm[i] = std::max(1, c->blocks_per_sm[i]);
     set(GPDA_OK);
     return c;
 }
@@ -1013,6 +1059,62 @@ int32_t gpda_run_host(gpda_ctx *c, int32_t mode, int32_t P, int32_t n, const flo
         CK(cudaMalloc(&c->dOff, sizeof(float) * (nph + kOffPad)));
         c->cap_ph = nph;
     }
+    c->has_offsets = off_idx != nullptr;
+    c->nph = nph;
+    c->mean_N = (double)nph / (double)B;
+    // Direct reads: in photon mode with one parameter set, page-locked host
+    // arrays are read by the kernel itself over the host link, each CTA
+    // staging its tile and writing it through to the store (PdaArgs::hN).
+    // One launch starts at once; the host link moves the store no faster
+    // than the copy engine, but the transfer now spreads over the whole
+    // simulation instead of preceding the first range's. Any other memory
+    // goes through the copy engine in burst ranges below.
+    if (mode == GPDA_MODE_PHOTON && P == 1) {
+        const void *hN = mapped_host(N, sizeof(int32_t) * (size_t)B);
+        const void *hT = mapped_host(T, sizeof(float) * (size_t)B);
+        const void *hOI = mapped_host(off_idx, sizeof(int64_t) * (size_t)(B + 1));
+        const void *hOff = nph > 0 ? mapped_host(offsets, sizeof(float) * (size_t)nph) : c->dOff;
+        auto aligned = [](const void *p, uintptr_t to) { return (reinterpret_cast<uintptr_t>(p) % to) == 0u; };
+        if (hN && hT && hOI && hOff && aligned(hN, 4) && aligned(hT, 4) && aligned(hOI, 8) &&
+            aligned(hOff, 16)) {
+            CK(cudaMemsetAsync(c->dFlag, 0, sizeof(unsigned int), c->stream));
+            CK(cudaMemsetAsync(c->dOff + nph, 0, sizeof(float) * kOffPad, c->stream));
+            c->B = B;
+            int rc = prepare_launch(c, mode, P, n, params);
+            PdaArgs a;
+            int grid = 0;
+            if (!rc) rc = range_args(c, mode, P, n, 0, B, S, seed, nullptr, c->has_obs, nullptr, a, grid);
+            if (rc) {
+                cudaStreamSynchronize(c->stream);
+                c->B = 0;
+                return rc;
+            }
+            grid = (int)std::min<int64_t>(a.n_items, (int64_t)c->num_sms * c->blocks_per_sm[kModePhotonDirect]);
+            a.vflag = c->dFlag;
+            a.nph = nph;
+            a.hN = static_cast<const int32_t *>(hN);
+            a.hT = static_cast<const float *>(hT);
+            a.hOffIdx = static_cast<const int64_t *>(hOI);
+            a.hOff = static_cast<const float *>(hOff);
+            a.wN = c->dN;
+            a.wT = c->dT;
+            a.wOffIdx = c->dOffIdx;
+            a.wOff = c->dOff;
+            CK(cudaMemsetAsync(c->dWork, 0, 2 * sizeof(unsigned int), c->stream));
+            CK(cudaEventRecord(c->k0, c->stream));
+            cudaError_t e = launch_pda(kModePhotonDirect, a, grid, sizeof(float) * kSmemCapFloats, c->stream);
+            if (e != cudaSuccess) {
+                cudaStreamSynchronize(c->stream);
+                c->B = 0;
+                return fail(c, GPDA_ERR_CUDA, cudaGetErrorString(e));
+            }
+            c->launches += 1;
+            CK(cudaEventRecord(c->k1, c->stream));
+            c->timed = true;
+            c->last_chi2 = c->has_obs;
+            return host_run_results(c, P, hist_out, chi2_out);
+        }
+    }
     while ((int)c->range_ev.size() < ranges) {
         cudaEvent_t e;
         CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
@@ -1027,9 +1129,6 @@ int32_t gpda_run_host(gpda_ctx *c, int32_t mode, int32_t P, int32_t n, const flo
         c->rjoin.push_back(e);
     }
     if (!c->prep_ev) CK(cudaEventCreateWithFlags(&c->prep_ev, cudaEventDisableTiming));
-    c->has_offsets = off_idx != nullptr;
-    c->nph = nph;
-    c->mean_N = (double)nph / (double)B;
     if (!off_idx) {
         double sumN = 0.0;
         for (int64_t b = 0; b < B; ++b) sumN += N[b];
@@ -1130,28 +1229,7 @@ int32_t gpda_run_host(gpda_ctx *c, int32_t mode, int32_t P, int32_t n, const flo
     CK(cudaEventRecord(c->k1, c->stream));
     c->timed = true;
     c->last_chi2 = c->has_obs;
-    const int nb = c->model.nbins;
-    CK(cudaMemcpyAsync(c->hFlag, c->dFlag, sizeof(unsigned int), cudaMemcpyDeviceToHost, c->stream));
-    if (hist_out) CK(cudaMemcpyAsync(c->hHist, c->dHist, sizeof(unsigned long long) * (size_t)P * nb, cudaMemcpyDeviceToHost, c->stream));
-    if (chi2_out && c->has_obs) CK(cudaMemcpyAsync(c->hChi2, c->dChi2, sizeof(double) * P, cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaStreamSynchronize(c->stream));
-    unsigned f = *c->hFlag;
-    if (f) {
-        c->B = 0;
-        std::string why;
-        if (f & 1u) why += " N outside [0, 2^21];";
-        if (f & 2u) why += " T not finite and >= 0;";
-        if (f & 4u) why += " off_idx inconsistent with N;";
-        if (f & 8u) why += " offset not finite;";
-        if (f & 16u) why += " offsets not sorted within a burst;";
-        return fail(c, GPDA_ERR_ARG, "burst store rejected:" + why);
-    }
-    if (hist_out) std::memcpy(hist_out, c->hHist, sizeof(uint64_t) * (size_t)P * nb);
-    if (chi2_out) {
-        if (c->has_obs) std::memcpy(chi2_out, c->hChi2, sizeof(double) * P);
-        else for (int p = 0; p < P; ++p) chi2_out[p] = NAN;
-    }
-    return GPDA_OK;
+    return host_run_results(c, P, hist_out, chi2_out);
 }
 
 int32_t gpda_expected_set_tape_limit(gpda_ctx *c, int64_t bytes) {

@@ -95,6 +95,21 @@ struct PdaArgs {
     // bits into *vflag and skips an item that fails
     unsigned int *vflag;
     int64_t nph;
+    // direct reads (launch mode kModePhotonDirect, one parameter set, vflag
+    // set): each CTA stages its tile from the caller's page-locked host
+    // arrays hN, hT, hOffIdx, hOff (device-mapped; naturally aligned, hOff
+    // to 16 bytes) instead of N, T, off_idx, offsets, checks it, and writes
+    // it through to the store (wN, wT, wOffIdx, wOff: the arrays behind N,
+    // T, off_idx, offsets) before it simulates, so the store is uploaded
+    // when the launch ends.
+    const int32_t *hN;
+    const float *hT;
+    const int64_t *hOffIdx;
+    const float *hOff;
+    int32_t *wN;
+    float *wT;
+    int64_t *wOffIdx;
+    float *wOff;
 };
 
 struct RcArgs {
@@ -115,7 +130,9 @@ struct RcArgs {
     float gamma, de, ct, r0;
 };
 
-// kernel launchers (gpda_kernels.cu)
+// kernel launchers (gpda_kernels.cu); launch mode kModePhotonDirect is photon
+// mode with direct reads of host arrays (PdaArgs::hN)
+constexpr int kModePhotonDirect = 2;
 cudaError_t launch_pda(int mode, const PdaArgs &a, int grid, size_t dyn_smem, cudaStream_t st);
 const void *pda_kernel_fn(int mode);   // the kernel launch_pda(mode) runs
 cudaError_t launch_chi2(const unsigned long long *hist, const float *obs, int P, int nbins,

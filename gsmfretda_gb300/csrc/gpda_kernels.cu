@@ -14,6 +14,9 @@
 //                      splits regrouped by sampler across the CTA. MODE 1: photon-by-photon
 //                      state assignment, one binomial per dwell segment,
 //                      drawn from tabulated CDFs (one 16-byte guide entry).
+//                      MODE 2: MODE 1 whose CTAs stage their tiles from the
+//                      caller's page-locked host arrays and write them
+//                      through to the burst store (gpda_run_host).
 //   binom_table_kernel the photon-mode CDF rows, one warp per row.
 //   chi2_kernel        reduced chi-square per parameter set, for callers that
 //                      launch without an observed histogram in the context.
@@ -30,6 +33,9 @@
 #include "gpda_internal.h"
 
 namespace gpda {
+
+// direct reads: host-memory loads each thread keeps in flight while staging
+constexpr int kStageBatch = 4;
 
 // number of offsets < x in the sorted range a[lo, hi)
 __device__ __forceinline__ int lower_bound(const float *a, int lo, int hi, float x) {
@@ -256,6 +262,11 @@ static __device__ __noinline__ void last_cta_chi2(const PdaArgs &a) {
 
 template <int MODE>
 __global__ void __launch_bounds__(kThreads, kMinBlocks) pda_kernel(const PdaArgs a) {
+    // MODE 2 is photon mode with direct reads of the caller's host arrays
+    // (PdaArgs::hN): its own instantiation, so that the staging code and its
+    // registers stay out of the resident photon kernel
+    constexpr bool kPhoton = MODE != 0;
+    constexpr bool direct = MODE == 2;
     extern __shared__ float4 s_ph4[];
     float *s_ph = reinterpret_cast<float *>(s_ph4);
     __shared__ DevParams sp;
@@ -281,7 +292,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) pda_kernel(const PdaArgs
     if (tid < kInvTable) s_inv[tid] = tid > 0 ? 1.0f / (float)tid : 0.0f;
     // photon mode: the background pair's constants (background_pair)
     __shared__ float s_bgc[4];
-    if (MODE == 1 && tid == 0) {
+    if (kPhoton && tid == 0) {
         const float bgs = a.bg_a + a.bg_d;
         const float pa = a.bg_a / bgs;
         s_bgc[0] = bgs;
@@ -290,6 +301,9 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) pda_kernel(const PdaArgs
         s_bgc[3] = 1.0f / (1.0f - pa);
     }
     const unsigned lt_mask = (1u << lane) - 1u;
+    // direct reads: the tile comes from the caller's host arrays and is
+    // written through to the store
+    __shared__ int64_t sOI[direct ? kMaxTileBursts + 1 : 1];   // the tile's off_idx
     int lim = 0;
     for (;;) {
         if (tid == 0) {
@@ -308,47 +322,124 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) pda_kernel(const PdaArgs
             uint32_t *dst = reinterpret_cast<uint32_t *>(&sp);
             for (int i = tid; i < kParamWords; i += kThreads) dst[i] = src[i];
         }
-        for (int i = tid; i < nb; i += kThreads) {
-            sN[i] = a.N[tb0 + i];
-            sT[i] = a.T[tb0 + i];
+        if (!direct) {
+            for (int i = tid; i < nb; i += kThreads) {
+                sN[i] = a.N[tb0 + i];
+                sT[i] = a.T[tb0 + i];
+            }
+        } else {
+            // host memory is microseconds away: N, T and off_idx of the tile
+            // in one round trip, off_idx kept in shared memory
+            for (int i = tid; i <= nb; i += kThreads) {
+                if (i < nb) {
+                    sN[i] = a.hN[tb0 + i];
+                    sT[i] = a.hT[tb0 + i];
+                }
+                sOI[i] = a.hOffIdx[tb0 + i];
+            }
+            __syncthreads();
         }
         for (int i = tid; i < a.nbins; i += kThreads) sh[i] = 0u;
-        if (MODE == 1 && a.vflag) {
+        if (kPhoton && a.vflag) {
             // the store's checks for the item's bursts (validate_kernel's),
-            // before the reads they bound; offsets follow once staged
+            // before the reads they bound; offsets follow once staged (direct
+            // reads: each thread checks the sN, sT entries it wrote itself)
             unsigned bad = 0u;
             for (int i = tid; i < nb; i += kThreads) {
-                const int32_t n_ = a.N[tb0 + i];
-                const float t_ = a.T[tb0 + i];
+                const int32_t n_ = direct ? sN[i] : a.N[tb0 + i];
+                const float t_ = direct ? sT[i] : a.T[tb0 + i];
                 if (n_ < 0 || n_ > (1 << 21)) bad |= 1u;
                 if (!(t_ >= 0.0f) || !isfinite(t_)) bad |= 2u;
-                const int64_t lo = a.off_idx[tb0 + i], hi = a.off_idx[tb0 + i + 1];
+                const int64_t lo = direct ? sOI[i] : a.off_idx[tb0 + i];
+                const int64_t hi = direct ? sOI[i + 1] : a.off_idx[tb0 + i + 1];
                 if (hi - lo != (int64_t)n_ || lo < 0 || hi > a.nph) bad |= 4u;
             }
             if (bad) atomicOr(a.vflag, bad);
             if (__syncthreads_or(bad != 0u)) continue;
         }
-        if (MODE == 1) {
+        if (kPhoton) {
             // Stage the tile's offsets: copy the 16-byte-aligned span that
             // covers [off_idx[tb0], off_idx[tb0+nb]) (the store is padded).
-            const int64_t first = a.off_idx[tb0];
-            const int64_t last = a.off_idx[tb0 + nb];
+            const int64_t first = direct ? sOI[0] : a.off_idx[tb0];
+            const int64_t last = direct ? sOI[nb] : a.off_idx[tb0 + nb];
             const int64_t abase = first & ~(int64_t)3;
             const int64_t aend = (last + 3) & ~(int64_t)3;
             const bool staged = (aend - abase) <= (int64_t)a.smem_cap;
             if (staged) {
-                for (int i = tid; i <= nb; i += kThreads) sOff[i] = (int32_t)(a.off_idx[tb0 + i] - abase);
-                const float4 *src = reinterpret_cast<const float4 *>(a.offsets + abase);
+                for (int i = tid; i <= nb; i += kThreads)
+                    sOff[i] = (int32_t)((direct ? sOI[i] : a.off_idx[tb0 + i]) - abase);
                 const int nv = (int)((aend - abase) >> 2);
-                for (int i = tid; i < nv; i += kThreads) s_ph4[i] = __ldg(src + i);
+                if (!direct) {
+                    const float4 *src = reinterpret_cast<const float4 *>(a.offsets + abase);
+                    for (int i = tid; i < nv; i += kThreads) s_ph4[i] = __ldg(src + i);
+                } else {
+                    // kStageBatch loads in flight per thread. The host array
+                    // is not padded: whole vectors below nph, the last one
+                    // element by element (zeros past nph, as in the store's
+                    // padding). The span's vectors go to the store too (its
+                    // ends overlap the neighbouring tiles' spans, which write
+                    // the same values).
+                    const float4 *src = reinterpret_cast<const float4 *>(a.hOff + abase);
+                    float4 *dst = reinterpret_cast<float4 *>(a.wOff + abase);
+                    for (int i0 = tid; i0 < nv; i0 += kStageBatch * kThreads) {
+                        float4 v[kStageBatch];
+#pragma unroll
+                        for (int u = 0; u < kStageBatch; ++u) {
+                            const int i = i0 + u * kThreads;
+                            const int64_t e = abase + 4 * (int64_t)i;
+                            if (i < nv && e + 4 <= a.nph) {
+                                v[u] = __ldg(src + i);
+                            } else {
+                                const bool in = i < nv;
+                                v[u].x = (in && e < a.nph) ? a.hOff[e] : 0.0f;
+                                v[u].y = (in && e + 1 < a.nph) ? a.hOff[e + 1] : 0.0f;
+                                v[u].z = (in && e + 2 < a.nph) ? a.hOff[e + 2] : 0.0f;
+                                v[u].w = 0.0f;
+                            }
+                        }
+#pragma unroll
+                        for (int u = 0; u < kStageBatch; ++u) {
+                            const int i = i0 + u * kThreads;
+                            if (i < nv) {
+                                s_ph4[i] = v[u];
+                                dst[i] = v[u];
+                            }
+                        }
+                    }
+                }
+            } else if (direct) {
+                // a tile too large to stage: copied to the store, from which
+                // this CTA then reads it
+                for (int64_t j0 = first + tid; j0 < last; j0 += kStageBatch * kThreads) {
+                    float v[kStageBatch];
+#pragma unroll
+                    for (int u = 0; u < kStageBatch; ++u) {
+                        const int64_t j = j0 + (int64_t)u * kThreads;
+                        v[u] = (j < last) ? a.hOff[j] : 0.0f;
+                    }
+#pragma unroll
+                    for (int u = 0; u < kStageBatch; ++u) {
+                        const int64_t j = j0 + (int64_t)u * kThreads;
+                        if (j < last) a.wOff[j] = v[u];
+                    }
+                }
+            }
+            if (direct) {
+                for (int i = tid; i <= nb; i += kThreads) {
+                    if (i < nb) {
+                        a.wN[tb0 + i] = sN[i];
+                        a.wT[tb0 + i] = sT[i];
+                    }
+                    a.wOffIdx[tb0 + i] = sOI[i];
+                }
             }
             if (tid == 0) s_staged = staged ? 1 : 0;
         }
         __syncthreads();
         const int units = nb * a.S;
-        const bool staged = (MODE == 1) && s_staged;
+        const bool staged = kPhoton && s_staged;
         const uint32_t pw = a.pbase + (uint32_t)p;
-        if (MODE == 1 && a.vflag) {
+        if (kPhoton && a.vflag) {
             // offsets finite and sorted within each burst; a warp per burst
             unsigned bad = 0u;
             for (int i = tid >> 5; i < nb; i += kThreads / 32) {
@@ -450,12 +541,12 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) pda_kernel(const PdaArgs
         // photon mode: one dwell segment per step; a lane whose unit is
         // finished takes the tile's next unit at once
         Unit U;
-        bool active = MODE == 1 && tid < units;
+        bool active = kPhoton && tid < units;
         if (active) unit_begin(U, tid, a.S, tb0, sN, sT, a.seed, pw);
         while (__any_sync(0xffffffffu, active)) {
             bool fin = false;
             int bin = -1;
-            if (MODE == 1 && active) {
+            if (kPhoton && active) {
                 fin = U.done;
                 if (!fin) {
                     const float *offs = staged ? (s_ph + sOff[U.lb]) : (a.offsets + a.off_idx[tb0 + U.lb]);
@@ -894,6 +985,7 @@ const void *pda_kernel_fn(int mode) {
 
 cudaError_t launch_pda(int mode, const PdaArgs &a, int grid, size_t dyn_smem, cudaStream_t st) {
     if (mode == 0) pda_kernel<0><<<grid, kThreads, dyn_smem, st>>>(a);
+    else if (mode == kModePhotonDirect) pda_kernel<2><<<grid, kThreads, dyn_smem, st>>>(a);
     else pda_kernel<1><<<grid, kThreads, dyn_smem, st>>>(a);
     return cudaGetLastError();
 }
@@ -905,6 +997,8 @@ cudaError_t pda_set_smem_limit(int mode, size_t dyn_smem) {
 
 cudaError_t pda_occupancy_blocks(int mode, size_t dyn_smem, int *blocks_per_sm) {
     if (mode == 0) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, pda_kernel<0>, kThreads, dyn_smem);
+    if (mode == kModePhotonDirect)
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, pda_kernel<2>, kThreads, dyn_smem);
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, pda_kernel<1>, kThreads, dyn_smem);
 }
 

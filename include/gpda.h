@@ -163,7 +163,13 @@ int64_t gpda_limit_hits(gpda_ctx *ctx);
  * kernels overlap. Every kernel reads the validation flag first and does
  * nothing once a range has been rejected. Results equal gpda_upload_bursts +
  * gpda_run_batched with the same arguments; the store stays uploaded for
- * later calls. A rejected store returns GPDA_ERR_ARG and leaves no store. */
+ * later calls. A rejected store returns GPDA_ERR_ARG and leaves no store.
+ * Direct reads: in photon mode with P = 1, when N, T, off_idx and offsets all
+ * lie in page-locked host memory (cudaHostAlloc, cudaMallocHost,
+ * cudaHostRegister; naturally aligned, offsets to 16 bytes), no copy is made
+ * and `ranges` is not used: one kernel reads the arrays over the host link,
+ * each CTA checking and staging its own bursts and writing them through to
+ * the device store, with the same results, checks and errors. */
 int32_t gpda_run_host(gpda_ctx *ctx, int32_t mode, int32_t P, int32_t n_states, const float *params,
                       const int32_t *N, const float *T, const int64_t *off_idx,
                       const float *offsets, int64_t B, int32_t samples, uint64_t seed,
