@@ -40,12 +40,9 @@ WORKLOAD = "photon_3state"
 B_FULL = 100_000
 SAMPLES = 100
 HELD_OUT_SEED = 0x0B5E
-# Algorithmic operations per unit of this workload, by the fixed cost model
-# (25 per 32-bit Philox word, 16 per log, 40 per binomial, 2 per photon
-# compare): D = 4.7 dwell segments per unit (mean exit rate ~2 x 1075 /s over
-# T ~ 1.7 ms) draw 1 + 2D + 4 + D words, D logs and D binomials, and N = 150
-# photons are compared once: (5 + 3D) 25 + 56 D + 2 N = 1,040.
-ALGO_OPS_PER_UNIT = 1040.0
+# Algorithmic operations per unit: the fixed cost model of
+# gsmfretda_gb300/roofline.py evaluated on the workload (its mean segments per
+# unit from the stationary jump flux of the parameter set, its mean photons).
 # Thread instructions the kernel issues per unit, from ncu (warp instructions x
 # active threads per instruction / units; profiles/pda_kernel_photon_3state.txt).
 ISSUED_INST_PER_UNIT = 1016.0
@@ -601,8 +598,10 @@ def main():
     alg_bytes = 4 * bs.B + 4 * bs.B + 8 * (bs.B + 1) + 4 * int(bs.off_idx[-1])
     hbm_peak, peak_kind, sm_max = peaks()
     achieved_gbs = alg_bytes / (kavg_ms * 1e-3) / 1e9
-    alu_peak = 152 * 128 * sm_max * 1e6 / 1e9          # FP32/INT32 lane-ops per s, in Gop/s
-    alu_achieved = units / (kavg_ms * 1e-3) * ALGO_OPS_PER_UNIT / 1e9
+    from gsmfretda_gb300 import roofline as rl
+    ops_per_unit, segs = rl.photon_ops_per_unit(n, args, bs.N, bs.T)
+    alu_peak = rl.lane_peak_gops(sm_max)               # FP32/INT32 lane-ops per s, in Gop/s
+    alu_achieved = units / (kavg_ms * 1e-3) * ops_per_unit / 1e9
     alu_issued = units / (kavg_ms * 1e-3) * ISSUED_INST_PER_UNIT / 1e9
 
     line = {
@@ -622,11 +621,13 @@ def main():
                      "traffic": NCU_TRAFFIC_BYTES if bs.B == B_FULL else None, "peak_kind": peak_kind,
                      "algorithmic_bytes_per_launch": alg_bytes, "kernel_ms": kavg_ms,
                      "alu": {"achieved": alu_achieved, "peak": alu_peak, "unit": "Gop/s",
-                             "frac": alu_achieved / alu_peak, "ops_per_unit": ALGO_OPS_PER_UNIT,
+                             "frac": alu_achieved / alu_peak, "ops_per_unit": ops_per_unit,
+                             "segments_per_unit": segs,
                              "issued": alu_issued, "issued_frac": alu_issued / alu_peak,
                              "issued_inst_per_unit": ISSUED_INST_PER_UNIT,
-                             "what": "algorithmic ops (cost model) and issued thread "
-                                     "instructions (ncu) vs 152 SMs x 128 lanes x SM clock"}},
+                             "what": "algorithmic ops (cost model of gsmfretda_gb300/roofline.py "
+                                     "on this workload) and issued thread instructions (ncu) vs "
+                                     "152 SMs x 128 lanes x SM clock"}},
         "chi2_last": float(chi2[0]),
     }
     if rank == 0 and world == 1 and not a.no_cpu_baseline:

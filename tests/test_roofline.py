@@ -1,0 +1,54 @@
+"""The ALU cost model the bench reports its roofline fraction against: the rate
+matrix layout, the stationary jump flux, and the mean segments per unit
+against a direct simulation of the same chain."""
+import numpy as np
+
+from gsmfretda_gb300 import roofline as rl
+from gsmfretda_gb300 import synth
+
+
+def test_rate_matrix_matches_the_parameter_layout():
+    rng = np.random.default_rng(3)
+    args = synth.random_3state_args(rng)
+    _, K, _ = synth.unpack_args(args, 3)
+    np.testing.assert_allclose(rl.rate_matrix(3, args), K)
+
+
+def test_two_state_segments_are_one_plus_rate_times_duration():
+    args = synth.pack_args([0.3, 0.72], [[0, 500.0], [500.0, 0]])
+    T = np.array([1e-3, 2e-3])
+    assert abs(rl.mean_segments(2, args, T) - (1.0 + 500.0 * 1.5e-3)) < 1e-9
+
+
+def _simulated_segments(K, T, rng):
+    n = K.shape[0]
+    kexit = K.sum(axis=0)
+    pi = rl.stationary(K)
+    total = 0
+    for Tb in T:
+        s = rng.choice(n, p=pi)
+        t, seg = 0.0, 1
+        while True:
+            t += rng.exponential(1.0 / kexit[s])
+            if t >= Tb:
+                break
+            seg += 1
+            s = rng.choice(n, p=K[:, s] / kexit[s])
+        total += seg
+    return total / len(T)
+
+
+def test_mean_segments_match_a_direct_simulation():
+    bs, n, args, md, S = synth.photon_3state(B=20000, seed=2)
+    K = rl.rate_matrix(n, args)
+    rng = np.random.default_rng(11)
+    sim = _simulated_segments(K, bs.T.astype(np.float64), rng)
+    D = rl.mean_segments(n, args, bs.T)
+    assert abs(sim - D) < 0.02 * D, (sim, D)
+
+
+def test_photon_ops_per_unit_formula():
+    bs, n, args, md, S = synth.photon_3state(B=2000, seed=2)
+    ops, D = rl.photon_ops_per_unit(n, args, bs.N, bs.T)
+    expect = 25 * (5 + 3 * D) + 56 * D + 2 * float(np.mean(bs.N))
+    assert abs(ops - expect) < 1e-9
