@@ -37,6 +37,35 @@ namespace gpda {
 // direct reads: host-memory loads each thread keeps in flight while staging
 constexpr int kStageBatch = 4;
 
+// Unsigned division by an invariant divisor (Granlund & Montgomery, "Division
+// by invariant integers using multiplication", PLDI 1994, fig. 4.1): for
+// 1 <= d < 2^31, l = ceil(log2 d) and m = floor(2^32 (2^l - d) / d) + 1 give
+// n / d = (t + ((n - t) >> min(l, 1))) >> max(l - 1, 0), t = umulhi(m, n),
+// for every 32-bit n. The kernels divide by the samples per burst (unit ->
+// burst, sample) and by a burst's photon count (its bin) once per unit.
+struct Divisor {
+    uint32_t m, l;
+};
+
+__device__ __forceinline__ Divisor divisor_of(uint32_t d) {
+    const uint32_t l = (d > 1u) ? 32u - (uint32_t)__clz((int)(d - 1u)) : 0u;
+    const uint64_t num = (uint64_t)((1ull << l) - d) << 32;
+    return Divisor{(uint32_t)(num / d + 1ull), l};
+}
+
+__device__ __forceinline__ uint32_t div_by(uint32_t n, uint32_t m, uint32_t l) {
+    const uint32_t t = __umulhi(m, n);
+    const uint32_t sh1 = l > 0u ? 1u : 0u;
+    const uint32_t sh2 = l > 0u ? l - 1u : 0u;
+    return (t + ((n - t) >> sh1)) >> sh2;
+}
+
+// a divisor kept in shared memory, read at each use (so that it does not hold
+// two registers across the simulation loop)
+__device__ __forceinline__ Divisor sdiv(const uint32_t &m, const uint32_t &l) {
+    return Divisor{*(const volatile uint32_t *)&m, *(const volatile uint32_t *)&l};
+}
+
 // number of offsets < x in the sorted range a[lo, hi)
 __device__ __forceinline__ int lower_bound(const float *a, int lo, int hi, float x) {
     while (lo < hi) {
@@ -59,9 +88,10 @@ struct Unit {
     bool done;
 };
 
-__device__ __forceinline__ void unit_begin(Unit &U, int u, int S, int64_t tb0, const int32_t *sN,
-                                           const float *sT, uint64_t seed, uint32_t pw) {
-    U.lb = u / S;
+__device__ __forceinline__ void unit_begin(Unit &U, int u, int S, Divisor dS, int64_t tb0,
+                                           const int32_t *sN, const float *sT, uint64_t seed,
+                                           uint32_t pw) {
+    U.lb = (int)div_by((uint32_t)u, dS.m, dS.l);
     U.s = u - U.lb * S;
     U.Nb = sN[U.lb];
     U.Tb = sT[U.lb];
@@ -273,6 +303,9 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) pda_kernel(const PdaArgs
     __shared__ int32_t sN[kMaxTileBursts];
     __shared__ float sT[kMaxTileBursts];
     __shared__ int32_t sOff[kMaxTileBursts + 1];
+    __shared__ uint32_t sNm[kMaxTileBursts];    // divisor_of(N) of the tile's bursts
+    __shared__ uint8_t sNl[kMaxTileBursts];
+    __shared__ uint32_t s_Sm, s_Sl;              // divisor_of(S)
     __shared__ unsigned int sh[kHistBins];
     __shared__ int s_item;
     __shared__ int s_staged;
@@ -286,7 +319,12 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) pda_kernel(const PdaArgs
     // may still change while later ranges are validated), so the whole CTA
     // takes the same branch.
     __shared__ int s_abort;
-    if (tid == 0) s_abort = (a.abort_flag && __ldcg(a.abort_flag) != 0u) ? 1 : 0;
+    if (tid == 0) {
+        s_abort = (a.abort_flag && __ldcg(a.abort_flag) != 0u) ? 1 : 0;
+        const Divisor dS = divisor_of((uint32_t)a.S);
+        s_Sm = dS.m;
+        s_Sl = dS.l;
+    }
     __syncthreads();
     if (s_abort) return;
     if (tid < kInvTable) s_inv[tid] = tid > 0 ? 1.0f / (float)tid : 0.0f;
@@ -338,6 +376,14 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) pda_kernel(const PdaArgs
                 sOI[i] = a.hOffIdx[tb0 + i];
             }
             __syncthreads();
+        }
+        // the bursts' divisors for binning (each thread reads the sN entries
+        // it wrote itself; the simulation reads them after a barrier)
+        for (int i = tid; i < nb; i += kThreads) {
+            const int32_t n_ = sN[i];
+            const Divisor d = divisor_of(n_ > 0 ? (uint32_t)n_ : 1u);
+            sNm[i] = d.m;
+            sNl[i] = (uint8_t)d.l;
         }
         for (int i = tid; i < a.nbins; i += kThreads) sh[i] = 0u;
         if (kPhoton && a.vflag) {
@@ -470,7 +516,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) pda_kernel(const PdaArgs
                 Unit U;
                 int bin = -1;
                 if (act) {
-                    unit_begin(U, u, a.S, tb0, sN, sT, a.seed, pw);
+                    unit_begin(U, u, a.S, sdiv(s_Sm, s_Sl), tb0, sN, sT, a.seed, pw);
                     if (!U.done)
                         while (!traj_occ(U, sp, a.r0, lim)) {
                         }
@@ -505,7 +551,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) pda_kernel(const PdaArgs
                     const int64_t b = tb0 + U.lb;
                     if (a.unit_out) a.unit_out[((int64_t)p * (a.b1 - a.b0) + (b - a.b0)) * a.S + U.s] = U.A;
                     if (U.Nb > 0 && U.A >= 0) {
-                        unsigned v = (unsigned)U.A * (unsigned)a.nbins / (unsigned)U.Nb;
+                        unsigned v = div_by((unsigned)U.A * (unsigned)a.nbins, sNm[U.lb], sNl[U.lb]);
                         bin = v >= (unsigned)a.nbins ? a.nbins - 1 : (int)v;
                     }
                 }
@@ -518,7 +564,8 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) pda_kernel(const PdaArgs
                     const int sig = (int)s_ent[1][tid];
                     const int ba = (int)s_ent[2][tid];
                     const float pe = __uint_as_float(s_ent[3][tid]);
-                    const int lb = ue / a.S, ss = ue - lb * a.S;
+                    const Divisor dS = sdiv(s_Sm, s_Sl);
+                    const int lb = (int)div_by((uint32_t)ue, dS.m, dS.l), ss = ue - lb * a.S;
                     Rng r;
                     r.init(a.seed, pw, (uint32_t)(tb0 + lb), (uint32_t)ss);
                     r.blk = s_ent[4][tid];
@@ -530,8 +577,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) pda_kernel(const PdaArgs
                     const int A = binom(r, sig, pe, lim, s_inv) + ba;
                     const int64_t b = tb0 + lb;
                     if (a.unit_out) a.unit_out[((int64_t)p * (a.b1 - a.b0) + (b - a.b0)) * a.S + ss] = A;
-                    const int Nb = sN[lb];
-                    unsigned v = (unsigned)A * (unsigned)a.nbins / (unsigned)Nb;
+                    unsigned v = div_by((unsigned)A * (unsigned)a.nbins, sNm[lb], sNl[lb]);
                     bin = v >= (unsigned)a.nbins ? a.nbins - 1 : (int)v;
                 }
                 hist_add_warp(sh, bin);
@@ -542,7 +588,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) pda_kernel(const PdaArgs
         // finished takes the tile's next unit at once
         Unit U;
         bool active = kPhoton && tid < units;
-        if (active) unit_begin(U, tid, a.S, tb0, sN, sT, a.seed, pw);
+        if (active) unit_begin(U, tid, a.S, sdiv(s_Sm, s_Sl), tb0, sN, sT, a.seed, pw);
         while (__any_sync(0xffffffffu, active)) {
             bool fin = false;
             int bin = -1;
@@ -560,6 +606,8 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) pda_kernel(const PdaArgs
                     const int64_t b = tb0 + U.lb;
                     if (a.unit_out) a.unit_out[((int64_t)p * (a.b1 - a.b0) + (b - a.b0)) * a.S + U.s] = U.A;
                     if (U.Nb > 0 && U.A >= 0) {
+                        // a hardware division here: the shared divisors cost this
+                        // loop a register spill
                         unsigned v = (unsigned)U.A * (unsigned)a.nbins / (unsigned)U.Nb;
                         bin = v >= (unsigned)a.nbins ? a.nbins - 1 : (int)v;
                     }
@@ -578,7 +626,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) pda_kernel(const PdaArgs
                 if (fin) {
                     const int u = base + __popc(need & lt_mask);
                     active = u < units;
-                    if (active) unit_begin(U, u, a.S, tb0, sN, sT, a.seed, pw);
+                    if (active) unit_begin(U, u, a.S, sdiv(s_Sm, s_Sl), tb0, sN, sT, a.seed, pw);
                 }
             }
         }

@@ -52,3 +52,4 @@ def test_photon_ops_per_unit_formula():
     ops, D = rl.photon_ops_per_unit(n, args, bs.N, bs.T)
     expect = 25 * (5 + 3 * D) + 56 * D + 2 * float(np.mean(bs.N))
     assert abs(ops - expect) < 1e-9
+
