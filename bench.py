@@ -45,10 +45,10 @@ HELD_OUT_SEED = 0x0B5E
 # unit from the stationary jump flux of the parameter set, its mean photons).
 # Thread instructions the kernel issues per unit, from ncu (warp instructions x
 # active threads per instruction / units; profiles/pda_kernel_photon_3state.txt).
-ISSUED_INST_PER_UNIT = 1016.0
+ISSUED_INST_PER_UNIT = 1000.0
 # DRAM bytes (read + write) of one MC launch on this workload, from the same
 # ncu capture; the algorithmic figure is computed live below.
-NCU_TRAFFIC_BYTES = 68.64e6
+NCU_TRAFFIC_BYTES = 68.36e6
 
 
 def parse():
