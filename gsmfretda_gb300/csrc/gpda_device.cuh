@@ -19,8 +19,12 @@ namespace gpda {
 constexpr int kMaxStates = 8;
 constexpr int kMaxSeg = 65536;      // segments per unit before the trajectory is cut
 constexpr int kMaxRestart = 256;    // rejection restarts before the sampler gives up
+// 1: Rng::align_now generates its block inline (the photon step's one block
+// per segment), every other draw site calls the out-of-line generator; 0:
+// all go out of line. Inline measured 0.664 -> 0.659 ms on the photon kernel
+// (e2e 0.796 -> 0.781 ms per gpda_run_host call), the same bits either way.
 #ifndef GPDA_ALIGN_INLINE
-#define GPDA_ALIGN_INLINE 0
+#define GPDA_ALIGN_INLINE 1
 #endif
 
 // ---------------------------------------------------------------- Philox
