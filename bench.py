@@ -43,7 +43,8 @@ HELD_OUT_SEED = 0x0B5E
 # Algorithmic operations per unit: the fixed cost model of
 # gsmfretda_gb300/roofline.py evaluated on the workload (its mean segments per
 # unit from the stationary jump flux of the parameter set, its mean photons).
-# Thread instructions the kernel issues per unit, from ncu (warp instructions x
+# Thread instructions the kernel issues per unit, from ncu (captured before the
+# segment's Philox block was generated inline; warp instructions x
 # active threads per instruction / units; profiles/pda_kernel_photon_3state.txt).
 ISSUED_INST_PER_UNIT = 1000.0
 # DRAM bytes (read + write) of one MC launch on this workload, from the same
