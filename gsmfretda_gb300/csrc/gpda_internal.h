@@ -95,6 +95,11 @@ struct PdaArgs {
     // bits into *vflag and skips an item that fails
     unsigned int *vflag;
     int64_t nph;
+    // resident photon mode: nonzero = the offsets array is exactly
+    // off_idx[b1] floats long (a caller's buffer, not the padded store), so
+    // the staged span's last vector is read element by element up to the
+    // tile's last photon instead of as one 16-byte load
+    int32_t exact_offsets;
     // direct reads (launch mode kModePhotonDirect, one parameter set, vflag
     // set): each CTA stages its tile from the caller's page-locked host
     // arrays hN, hT, hOffIdx, hOff (device-mapped; naturally aligned, hOff

@@ -417,7 +417,24 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) pda_kernel(const PdaArgs
                 const int nv = (int)((aend - abase) >> 2);
                 if (!direct) {
                     const float4 *src = reinterpret_cast<const float4 *>(a.offsets + abase);
-                    for (int i = tid; i < nv; i += kThreads) s_ph4[i] = __ldg(src + i);
+                    // an exactly sized array ends at a photon of some tile:
+                    // whole vectors below the tile's last photon, the last
+                    // one element by element (zeros past it, which no burst
+                    // of this tile reads)
+                    const int64_t vend = a.exact_offsets ? last : INT64_MAX;
+                    for (int i = tid; i < nv; i += kThreads) {
+                        const int64_t e = abase + 4 * (int64_t)i;
+                        float4 v;
+                        if (e + 4 <= vend) {
+                            v = __ldg(src + i);
+                        } else {
+                            v.x = (e < vend) ? a.offsets[e] : 0.0f;
+                            v.y = (e + 1 < vend) ? a.offsets[e + 1] : 0.0f;
+                            v.z = (e + 2 < vend) ? a.offsets[e + 2] : 0.0f;
+                            v.w = 0.0f;
+                        }
+                        s_ph4[i] = v;
+                    }
                 } else {
                     // kStageBatch loads in flight per thread. The host array
                     // is not padded: whole vectors below nph, the last one
@@ -1040,6 +1057,8 @@ cudaError_t launch_pda(int mode, const PdaArgs &a, int grid, size_t dyn_smem, cu
 
 cudaError_t pda_set_smem_limit(int mode, size_t dyn_smem) {
     if (mode == 0) return cudaFuncSetAttribute(pda_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn_smem);
+    if (mode == kModePhotonDirect)
+        return cudaFuncSetAttribute(pda_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn_smem);
     return cudaFuncSetAttribute(pda_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn_smem);
 }
 

@@ -22,10 +22,16 @@
 // it and must be serialised by the caller (one stream, or events).
 // The first call on a device looks up the array's device address with
 // cudaGetSymbolAddress while that device is current; make that first call
-// before any stream capture that should contain a later call.
+// before any stream capture begins.
+// The caller's arrays are read in place: offsets must start on a 16-byte
+// boundary (the photon staging reads it as float4), and it may be exactly
+// off_idx[B] floats long (the last vector of every tile is read element by
+// element). Units whose bounded loops hit their limit are counted in the
+// scratch but not reported by this entry point.
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdint>
 #include <cstring>
 #include <mutex>
 
@@ -101,6 +107,11 @@ extern "C" int32_t gpda_run_pda_noalloc(const gpda_model *m, int32_t mode, int32
     if (n_states < 1 || n_states > GPDA_MAX_STATES || samples < 1 || !params) return GPDA_ERR_ARG;
     if (!N || !T || !hist || B < 1 || B * (int64_t)samples > (int64_t)INT32_MAX) return GPDA_ERR_ARG;
     if (mode == GPDA_MODE_PHOTON && (!off_idx || !offsets)) return GPDA_ERR_ARG;
+    auto aligned = [](const void *p, uintptr_t to) { return (reinterpret_cast<uintptr_t>(p) % to) == 0u; };
+    if (!aligned(N, 4) || !aligned(T, 4) || !aligned(hist, 8) || (chi2 && !aligned(chi2, 8)) ||
+        (ohist && !aligned(ohist, 4)))
+        return GPDA_ERR_ARG;
+    if (mode == GPDA_MODE_PHOTON && (!aligned(off_idx, 8) || !aligned(offsets, 16))) return GPDA_ERR_ARG;
     if (mode == GPDA_MODE_PHOTON && P * n_states > kNoAllocMaxTables) return GPDA_ERR_ARG;
     if ((ohist == nullptr) != (chi2 == nullptr)) return GPDA_ERR_ARG;
     if (mm.nbins < 1 || mm.nbins > GPDA_MAX_BINS || mm.left_pad < 0 || mm.left_pad > mm.nbins ||
@@ -145,6 +156,7 @@ extern "C" int32_t gpda_run_pda_noalloc(const gpda_model *m, int32_t mode, int32
     a.T = T;
     a.off_idx = off_idx;
     a.offsets = offsets;
+    a.exact_offsets = 1;          // the caller's array need not be padded
     a.params = sc->params;
     a.hist = reinterpret_cast<unsigned long long *>(hist);
     a.unit_out = nullptr;

@@ -240,18 +240,21 @@ int32_t gpda_expected_grad(gpda_ctx *ctx, int32_t P, int32_t n_states, const flo
  * allocator owns the device memory, or a loop that must not pay cudaMalloc's
  * implicit synchronisation): runs the same Monte-Carlo kernel as
  * gpda_run_batched over bursts [0,B) of caller-owned DEVICE arrays (N, T and,
- * for photon mode, off_idx/offsets, laid out and valid as gpda_upload_bursts
- * requires; not re-validated here) and writes P*nbins counts into the DEVICE
- * array hist (zeroed first); with ohist/chi2 (device, nbins floats / P
- * doubles) it also writes the reduced chi-square. params is a HOST array of
- * P*n(n+1) floats. Allocates nothing: its scratch is a fixed array of about
- * 21 MB inside the library, held by every device that loads it until exit,
- * which limits P to 64, and in photon mode P*n_states to 8 (GPDA_ERR_ARG
- * beyond). Runs asynchronously on `stream`
- * (a cudaStream_t, NULL = legacy default stream) on the current device.
- * Calls share the scratch: calls that overlap on the GPU race and must be
- * serialised by the caller. The first call on a device looks up the scratch
- * address with that device current; make it before any stream capture. */
+ * for photon mode, off_idx/offsets, with the layout and values
+ * gpda_upload_bursts accepts; not re-validated here) and writes P*nbins
+ * counts into the DEVICE array hist (zeroed first); with ohist/chi2 (device,
+ * nbins floats / P doubles) it also writes the reduced chi-square. params is
+ * a HOST array of P*n(n+1) floats. Arrays are naturally aligned and offsets
+ * starts on a 16-byte boundary (GPDA_ERR_ARG otherwise); offsets may be
+ * exactly off_idx[B] floats long. Allocates nothing: its scratch is a fixed
+ * array of about 21 MB inside the library, held by every device that loads
+ * it until exit, which limits P to 64, and in photon mode P*n_states to 8
+ * (GPDA_ERR_ARG beyond). Runs asynchronously on `stream` (a cudaStream_t,
+ * NULL = legacy default stream) on the current device. Calls share the
+ * scratch: calls that overlap on the GPU race and must be serialised by the
+ * caller. The first call on a device looks up the scratch address with that
+ * device current; make it before any stream capture begins. Loop-limit hits
+ * (gpda_limit_hits on a context) are not reported by this entry point. */
 int32_t gpda_run_pda_noalloc(const gpda_model *m, int32_t mode, int32_t P, int32_t n_states,
                              const float *params, const int32_t *N, const float *T,
                              const int64_t *off_idx, const float *offsets, int64_t B,
