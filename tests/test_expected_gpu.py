@@ -5,8 +5,26 @@ device forward (h = 1e-4), and through the torch.autograd.Function.
 
 Tolerances: normalised bin masses within 1e-5 absolute (device masses are
 FP32 with the Loader/recurrence evaluation, the oracle's exact FP64); reduced
-chi-square within 1e-5 relative; gradients within 1e-3 of the largest
-component."""
+chi-square within 1e-5 relative; gradients within 1e-3 relative, component
+by component, for every component above a floor of 1e-3 of the largest (a
+component below the floor is held to 1e-3 of the largest instead), and
+within 1e-3 of the largest component as a second bar."""
+
+GRAD_RTOL = 1e-3      # per component, relative to the reference value
+GRAD_FLOOR = 1e-3     # components below GRAD_FLOOR * max |reference| are compared absolutely
+
+
+def _assert_grad_close(g, ref, what):
+    """|g_k - ref_k| <= GRAD_RTOL |ref_k| for |ref_k| >= GRAD_FLOOR max|ref|,
+    and |g_k - ref_k| <= GRAD_RTOL max|ref| for every k."""
+    g = np.asarray(g, dtype=np.float64)
+    ref = np.asarray(ref, dtype=np.float64)
+    scale = np.abs(ref).max()
+    err = np.abs(g - ref)
+    big = np.abs(ref) >= GRAD_FLOOR * scale
+    rel = np.where(big, err / np.maximum(np.abs(ref), 1e-300), 0.0)
+    assert np.all(rel <= GRAD_RTOL), f"{what}: per-component relative error {rel} (g={g}, ref={ref})"
+    assert err.max() <= GRAD_RTOL * scale, f"{what}: error {err} vs scale {scale}"
 import numpy as np
 import pytest
 
@@ -50,7 +68,7 @@ def test_forward_and_adjoint_match_the_oracle(orc, gpda_lib, n):
     assert np.abs(H - Ho).max() / units < 1e-5
     assert abs(c[0] - co[0]) <= 1e-5 * abs(co[0])
     g, go = np.concatenate([dE[0], dK[0]]), np.concatenate([eo[0], ko[0]])
-    assert np.abs(g - go).max() <= 1e-3 * np.abs(go).max(), (g, go)
+    _assert_grad_close(g, go, "adjoint vs FP64 oracle")
     # the fused call gives the same numbers (same kernels, fixed summation order)
     np.testing.assert_array_equal(H2, H)
     np.testing.assert_array_equal(c2, c)
@@ -81,9 +99,8 @@ def test_full_size_gradient_vs_oracle_and_central_differences(orc, gpda_lib):
             _, cm = eng.expected_hist(n, am, S, 5, anchor=th)
             fd[k] = (cp[0] - cm[0]) / step
     assert abs(c[0] - co[0]) <= 1e-5 * abs(co[0])
-    scale = np.abs(go).max()
-    assert np.abs(g - go).max() <= 1e-3 * scale, (g, go)
-    assert np.abs(g - fd).max() <= 1e-3 * scale, (g, fd)
+    _assert_grad_close(g, go, "adjoint vs FP64 oracle")
+    _assert_grad_close(g, fd, "adjoint vs central differences")
 
 
 def test_population_batch_matches_the_oracle(orc, gpda_lib):
@@ -99,7 +116,7 @@ def test_population_batch_matches_the_oracle(orc, gpda_lib):
     np.testing.assert_allclose(c, co, rtol=1e-5)
     g, go = np.concatenate([dE, dK], 1), np.concatenate([eo, ko], 1)
     for p in range(P):
-        assert np.abs(g[p] - go[p]).max() <= 1e-3 * np.abs(go[p]).max()
+        _assert_grad_close(g[p], go[p], f"set {p}: adjoint vs FP64 oracle")
 
 
 def test_autograd_function(orc, gpda_lib):

@@ -46,6 +46,10 @@ def test_gradient_matches_central_differences(orc, n):
         fd[k] = (cp[0] - cm[0]) / step
     scale = np.abs(fd).max()
     assert np.abs(g - fd).max() <= 1e-4 * scale, (g, fd)
+    # component by component: 1e-3 relative above a floor of 1e-3 of the largest
+    big = np.abs(fd) >= 1e-3 * scale
+    rel = np.abs(g - fd)[big] / np.abs(fd)[big]
+    assert np.all(rel <= 1e-3), (rel, g, fd)
 
 
 def test_anchor_equal_to_params_is_the_plain_form(orc):
