@@ -15,7 +15,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 def build(verbose: bool = False) -> str:
     src = os.path.join(HERE, "gpda_oracle.c")
     out = os.path.join(HERE, "liborc.so")
-    deps = [src, os.path.join(HERE, "gpda_oracle_core.inc"), os.path.join(HERE, "gpda_oracle.h")]
+    deps = [src, os.path.join(HERE, "gpda_oracle_core.inc"), os.path.join(HERE, "rc_unit_body.inc"),
+            os.path.join(HERE, "gpda_oracle.h")]
     if os.path.exists(out) and all(os.path.getmtime(out) >= os.path.getmtime(d) for d in deps):
         return out
     cmd = ["gcc", "-O3", "-std=c11", "-fopenmp", "-ffp-contract=off", "-fno-fast-math",

@@ -502,6 +502,219 @@ static void binom_cdf_row_d(double pp, int nn, double *out) {
 #define INV_T inv_tab_f
 #define PFX(x) f32_##x
 #include "gpda_oracle_core.inc"
+
+static void init_lf_d(void);
+
+/* ---------------- replay of the reference kernel's recorded draws ----------------
+ * The reference-kernel harness (oracle/mcref_harness.cu, built from the
+ * reference's own mc_kernel, gen_rand.cuh and binom.cuh) records, per thread,
+ * every draw mc_kernel's helpers make: the Sobol uniforms, drawTau's value,
+ * the Poisson variates with their means, the normal and drawE's value, and
+ * rk_binomial's (n, p, result). orc_rc_replay runs the oracle's own
+ * mc_kernel body (rc_unit_body.inc, the same text unit_rc runs on Philox
+ * draws) on those records and compares its mcE with the reference's. */
+typedef struct {
+    const orc_tape_rec *rec;
+    int64_t len, pos;
+    int32_t off_path;           /* a record of the wrong kind, or none left */
+    orc_replay_stats *st;
+} tape_src;
+
+static const orc_tape_rec *tape_next(tape_src *t, int kind) {
+    static const orc_tape_rec none = {0, 0, 0.0};
+    if (t->off_path || t->pos >= t->len || (t->rec[t->pos].tag & 0xff) != kind) {
+        t->off_path = 1;
+        return &none;
+    }
+    return &t->rec[t->pos++];
+}
+
+static float tape_u(tape_src *t) { return (float)tape_next(t, ORC_TAPE_U)->d; }
+
+static uint32_t f32_bits(float x) {
+    uint32_t u;
+    memcpy(&u, &x, 4);
+    return u;
+}
+
+/* drawTau: the reference's value is used; the oracle's log of the same
+ * uniform is compared with it in ulps */
+static float tape_tau(tape_src *t, float k) {
+    const float u = tape_u(t);
+    const float ours = orc_logf(u) / (-k);
+    const float ref = (float)tape_next(t, ORC_TAPE_TAU)->d;
+    if (t->off_path) return INFINITY;   /* ends the trajectory: the unit is reported off path */
+    {
+        int64_t d = (int64_t)f32_bits(ours) - (int64_t)f32_bits(ref);
+        if (d < 0) d = -d;
+        if (d > t->st->tau_max_ulp) t->st->tau_max_ulp = d;
+    }
+    return ref;
+}
+
+/* draw_P_B_Tr for one time bin: the clip rule on the reference's Poisson
+ * variate; its mean must be the float tdiff * rate the body computed */
+static float tape_bg(tape_src *t, float tot, float tdiff, float rate) {
+    const orc_tape_rec *p = tape_next(t, ORC_TAPE_P);
+    const float lam = tdiff * rate;
+    if (!t->off_path && (double)lam != p->d) t->st->lambda_mismatch += 1;
+    const int sv = p->i;
+    if ((float)sv <= tot) return (float)sv;
+    return floorf(tot * tape_u(t));
+}
+
+/* drawE: the reference's value is used; the oracle's formula on the same
+ * normal is compared with it */
+static float tape_e(tape_src *t, float e, float r0, float v) {
+    const float z = (float)tape_next(t, ORC_TAPE_N)->d;
+    const float ours = f32_broaden_z(z, e, r0, v);
+    const float ref = (float)tape_next(t, ORC_TAPE_E)->d;
+    if (!t->off_path) {
+        double d = fabs((double)ours - (double)ref);
+        if (d > t->st->e_max_abs) t->st->e_max_abs = d;
+    }
+    return ref;
+}
+
+/* rk_binomial: the reference's variate; its (n, p) must be the body's */
+static int64_t tape_binom(tape_src *t, int n, float p) {
+    const orc_tape_rec *b = tape_next(t, ORC_TAPE_B);
+    if (!t->off_path && ((b->tag >> 8) != n || b->d != (double)p)) t->st->binom_arg_mismatch += 1;
+    return b->i;
+}
+
+#define RC_U(src) tape_u(src)
+#define RC_TAU(src, k) tape_tau(src, k)
+#define RC_BG(src, tot, tdiff, rate) tape_bg(src, tot, tdiff, rate)
+#define RC_E(src, e, r0, v) tape_e(src, e, r0, v)
+#define RC_BINOM(src, n, p) tape_binom(src, n, p)
+static float f32_unit_rc_tape(const f32_tab *tb, const orc_rc_bursts *bs, const orc_model *m,
+                              int64_t b, tape_src *src) {
+#include "rc_unit_body.inc"
+}
+#undef RC_U
+#undef RC_TAU
+#undef RC_BG
+#undef RC_E
+#undef RC_BINOM
+
+/* The tape format's self-check: the oracle's own Philox draws written as the
+ * harness writes the reference's (orc_rc_record), so that replaying them must
+ * give unit_rc's values bit for bit. */
+typedef struct {
+    orc_rng r;
+    orc_tape_rec *rec;
+    int64_t len, cap;
+} tape_sink;
+
+static void sink_put(tape_sink *k, int32_t tag, int32_t i, double d) {
+    if (k->len < k->cap) {
+        k->rec[k->len].tag = tag;
+        k->rec[k->len].i = i;
+        k->rec[k->len].d = d;
+    }
+    k->len += 1;
+}
+static float sink_u(tape_sink *k) {
+    const float u = f32_u01(&k->r);
+    sink_put(k, ORC_TAPE_U, 0, (double)u);
+    return u;
+}
+static float sink_tau(tape_sink *k, float kk) {
+    const float v = orc_logf(sink_u(k)) / (-kk);
+    sink_put(k, ORC_TAPE_TAU, 0, (double)v);
+    return v;
+}
+static float sink_bg(tape_sink *k, float tot, float tdiff, float rate) {
+    const float lam = tdiff * rate;
+    const int sv = f32_poisson(&k->r, lam);
+    sink_put(k, ORC_TAPE_P, sv, (double)lam);
+    if ((float)sv <= tot) return (float)sv;
+    return floorf(tot * sink_u(k));
+}
+static float sink_e(tape_sink *k, float e, float r0, float v) {
+    const float z = f32_normal(&k->r);
+    sink_put(k, ORC_TAPE_N, 0, (double)z);
+    const float x = f32_broaden_z(z, e, r0, v);
+    sink_put(k, ORC_TAPE_E, 0, (double)x);
+    return x;
+}
+static int64_t sink_binom(tape_sink *k, int n, float p) {
+    const int v = f32_binom(&k->r, n, p);
+    sink_put(k, ORC_TAPE_B | (n << 8), v, (double)p);
+    return v;
+}
+#define RC_U(src) sink_u(src)
+#define RC_TAU(src, k) sink_tau(src, k)
+#define RC_BG(src, tot, tdiff, rate) sink_bg(src, tot, tdiff, rate)
+#define RC_E(src, e, r0, v) sink_e(src, e, r0, v)
+#define RC_BINOM(src, n, p) sink_binom(src, n, p)
+static float f32_unit_rc_record(const f32_tab *tb, const orc_rc_bursts *bs, const orc_model *m,
+                                int64_t b, tape_sink *src) {
+#include "rc_unit_body.inc"
+}
+#undef RC_U
+#undef RC_TAU
+#undef RC_BG
+#undef RC_E
+#undef RC_BINOM
+
+int orc_rc_record(const orc_rc_bursts *bs, int32_t n, const float *args, const orc_model *m,
+                  int32_t R, uint64_t seed, int32_t cap, orc_tape_rec *tape, int32_t *tape_len,
+                  float *mcE_out) {
+    if (!bs || !args || !m || !tape || !tape_len || !mcE_out || n < 2 || n > ORC_MAXS || R < 1 || cap < 0)
+        return -1;
+    init_lf_d();
+    f32_tab tb;
+    int rc = f32_build(n, args, m, &tb, 0);
+    if (rc != 0) return rc;
+    for (int64_t t = 0; t < bs->B * (int64_t)R; ++t) {
+        tape_sink k;
+        rng_init(&k.r, seed, 0u, (uint32_t)(t / R), (uint32_t)(t % R));
+        k.rec = tape + t * (int64_t)cap;
+        k.len = 0;
+        k.cap = cap;
+        mcE_out[t] = f32_unit_rc_record(&tb, bs, m, t / R, &k);
+        tape_len[t] = (int32_t)k.len;
+    }
+    return 0;
+}
+
+int orc_rc_replay(const orc_rc_bursts *bs, int32_t n, const float *args, const orc_model *m,
+                  int32_t R, const orc_tape_rec *tape, const int32_t *tape_len, int32_t cap,
+                  const float *ref_mcE, float *mcE_out, int8_t *status_out,
+                  orc_replay_stats *stats) {
+    if (!bs || !args || !m || !tape || !tape_len || !ref_mcE || !stats || n < 2 || n > ORC_MAXS ||
+        R < 1 || cap < 0)
+        return -1;
+    init_lf_d();
+    f32_tab tb;
+    int rc = f32_build(n, args, m, &tb, 0);
+    if (rc != 0) return rc;
+    memset(stats, 0, sizeof(*stats));
+    const int64_t units = bs->B * (int64_t)R;
+    stats->units = units;
+    for (int64_t t = 0; t < units; ++t) {
+        const int64_t b = t / R;
+        int8_t status;
+        float x = 0.0f;
+        if (tape_len[t] > cap) {
+            status = ORC_REPLAY_TRUNCATED;
+        } else {
+            tape_src src = {tape + t * (int64_t)cap, tape_len[t], 0, 0, stats};
+            x = f32_unit_rc_tape(&tb, bs, m, b, &src);
+            if (src.off_path || src.pos != src.len) status = ORC_REPLAY_OFF_PATH;
+            else status = (f32_bits(x) == f32_bits(ref_mcE[t])) ? ORC_REPLAY_EXACT : ORC_REPLAY_DIFFERS;
+        }
+        if (mcE_out) mcE_out[t] = x;
+        if (status_out) status_out[t] = status;
+        if (status == ORC_REPLAY_EXACT) stats->exact += 1;
+        else if (status == ORC_REPLAY_DIFFERS) stats->differs += 1;
+        else if (status == ORC_REPLAY_TRUNCATED) stats->truncated += 1;
+        else stats->off_path += 1;
+    }
+    return 0;
+}
 #undef REAL
 #undef RL
 #undef LOGR
@@ -590,6 +803,26 @@ int orc_sample(int kind, uint64_t seed, int32_t n, float p, int64_t count, doubl
         case 6: out[i] = (double)f64_poisson(&r, (double)p); break;
         default: return -1;
         }
+    }
+    return 0;
+}
+
+/* the photon-mode background pair (background_pair) without clipping:
+ * variate i = (A_i, D_i) on the unit stream of counter (0, 0, i), with the
+ * kernel's constants for rates (bg_a, bg_d) over a segment of length dt */
+int orc_sample_bgpair(uint64_t seed, float bg_a, float bg_d, float dt, int64_t count, int32_t *A,
+                      int32_t *D) {
+    if (!A || !D || !(bg_a > 0.0f) || !(bg_d > 0.0f) || !(dt >= 0.0f)) return -1;
+    init_lf_d();
+    const float bgs = bg_a + bg_d;
+    const float pa = bg_a / bgs;
+    const float bgc[4] = {bgs, pa, 1.0f / pa, 1.0f / (1.0f - pa)};
+    for (int64_t i = 0; i < count; ++i) {
+        orc_rng r;
+        rng_init(&r, seed, 0u, 0u, (uint32_t)i);
+        int rem = 0;
+        A[i] = f32_background_pair(&r, 1 << 30, dt, bgc, &rem);
+        D[i] = (1 << 30) - rem - A[i];
     }
     return 0;
 }

@@ -111,6 +111,10 @@ float orc_cos2pif(float u);
  * 2 exponential(rate=lam) 3 normal 4 u01  */
 int orc_sample(int kind, uint64_t seed, int32_t n, float p, int64_t count, double *out);
 
+/* photon-mode background pair (A, D) without clipping, `count` variates */
+int orc_sample_bgpair(uint64_t seed, float bg_a, float bg_d, float dt, int64_t count, int32_t *A,
+                      int32_t *D);
+
 /* categorical draws (mode 0 pda cumulative, 1 drawDisIdx weights, 2 pda jump
  * row, 3 drawJ_Si2Sj column-major matrix); variate i uses sample word i */
 int orc_sample_cat(uint64_t seed, int32_t mode, int32_t n, const float *w, int32_t from,
@@ -158,6 +162,46 @@ void orc_bin_values(const float *x, int64_t n, int32_t nbins, float *hist_out);
 int orc_expected(const orc_bursts *bs, int32_t n, const float *params, const float *anchor,
                  int32_t P, const orc_model *m, int32_t S, uint64_t seed, const float *obs,
                  double *hist, double *chi2, double *dE, double *dlogK, int32_t nthreads);
+
+/* Replay of the reference kernel's recorded draws (mc_kernel, src/mc.cu:83-197,
+ * run by oracle/mcref_harness.cu). One record per draw of a thread, in
+ * order; tag & 0xff is the kind, tag >> 8 the binomial's n.
+ *   U    d = the Sobol uniform (drawDisIdx, drawJ_Si2Sj, drawTau, the clip of draw_P_B_Tr)
+ *   TAU  d = drawTau's value
+ *   N    d = curand_normal's value (drawE)
+ *   E    d = drawE's value
+ *   P    i = curand_poisson's value, d = its mean (draw_P_B_Tr)
+ *   B    i = rk_binomial's value, d = its p, tag >> 8 = its n */
+enum { ORC_TAPE_U = 1, ORC_TAPE_TAU = 2, ORC_TAPE_N = 3, ORC_TAPE_E = 4, ORC_TAPE_P = 5,
+       ORC_TAPE_B = 6 };
+typedef struct {
+    int32_t tag;
+    int32_t i;
+    double d;
+} orc_tape_rec;
+enum { ORC_REPLAY_EXACT = 0, ORC_REPLAY_DIFFERS = 1, ORC_REPLAY_TRUNCATED = 2,
+       ORC_REPLAY_OFF_PATH = 3 };
+typedef struct {
+    int64_t units, exact, differs, truncated, off_path;
+    int64_t lambda_mismatch;      /* Poisson means unlike the body's tdiff * rate */
+    int64_t binom_arg_mismatch;   /* binomial (n, p) unlike the body's */
+    int64_t tau_max_ulp;          /* oracle log vs the reference's drawTau */
+    double e_max_abs;             /* oracle drawE formula vs the reference's */
+} orc_replay_stats;
+/* Thread t = b * R + s (R a power of two, as mc_kernel requires) has
+ * tape_len[t] records at tape[t * cap]; tape_len[t] > cap means its tape
+ * was cut. mcE_out / status_out (nullable) per thread. */
+int orc_rc_replay(const orc_rc_bursts *bs, int32_t n, const float *args, const orc_model *m,
+                  int32_t R, const orc_tape_rec *tape, const int32_t *tape_len, int32_t cap,
+                  const float *ref_mcE, float *mcE_out, int8_t *status_out,
+                  orc_replay_stats *stats);
+
+/* The oracle's own Philox draws of mc_kernel units (seed and counters as
+ * orc_run_refcompat uses them) written in the tape format: a self-check of
+ * the replay, whose result must equal the recorded mcE_out bit for bit. */
+int orc_rc_record(const orc_rc_bursts *bs, int32_t n, const float *args, const orc_model *m,
+                  int32_t R, uint64_t seed, int32_t cap, orc_tape_rec *tape, int32_t *tape_len,
+                  float *mcE_out);
 
 #ifdef __cplusplus
 }

@@ -40,6 +40,17 @@ class OrcRcBursts(C.Structure):
                 ("bg_ad_rate", C.c_float), ("bg_dd_rate", C.c_float)]
 
 
+class OrcReplayStats(C.Structure):
+    _fields_ = [("units", C.c_int64), ("exact", C.c_int64), ("differs", C.c_int64),
+                ("truncated", C.c_int64), ("off_path", C.c_int64), ("lambda_mismatch", C.c_int64),
+                ("binom_arg_mismatch", C.c_int64), ("tau_max_ulp", C.c_int64),
+                ("e_max_abs", C.c_double)]
+
+
+# one draw record of the tape format (orc_tape_rec): kind | n << 8, integer, double
+TAPE_DTYPE = np.dtype([("tag", np.int32), ("i", np.int32), ("d", np.float64)])
+TAPE_U, TAPE_TAU, TAPE_N, TAPE_E, TAPE_P, TAPE_B = 1, 2, 3, 4, 5, 6
+
 _lib = None
 
 
@@ -77,6 +88,15 @@ def lib():
                                       C.c_int32]
         _lib.orc_bin_values.argtypes = [C.c_void_p, C.c_int64, C.c_int32, C.c_void_p]
         _lib.orc_philox4x32_10.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        _lib.orc_sample_bgpair.argtypes = [C.c_uint64, C.c_float, C.c_float, C.c_float, C.c_int64,
+                                           C.c_void_p, C.c_void_p]
+        _lib.orc_rc_replay.argtypes = [C.POINTER(OrcRcBursts), C.c_int32, C.c_void_p,
+                                       C.POINTER(OrcModel), C.c_int32, C.c_void_p, C.c_void_p,
+                                       C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p,
+                                       C.POINTER(OrcReplayStats)]
+        _lib.orc_rc_record.argtypes = [C.POINTER(OrcRcBursts), C.c_int32, C.c_void_p,
+                                       C.POINTER(OrcModel), C.c_int32, C.c_uint64, C.c_int32,
+                                       C.c_void_p, C.c_void_p, C.c_void_p]
     return _lib
 
 
@@ -172,6 +192,63 @@ def run_refcompat(rc_data, n, args, m, S, seed, b0=0, b1=None, want_mcE=True, nt
     if rc != 0:
         raise ValueError(f"orc_run_refcompat rc={rc}")
     return hist, mcE
+
+
+def sample_bgpair(seed, bg_a, bg_d, dt, count):
+    """(A, D) variates of the photon-mode background pair, unclipped."""
+    A = np.zeros(count, dtype=np.int32)
+    D = np.zeros(count, dtype=np.int32)
+    rc = lib().orc_sample_bgpair(seed, bg_a, bg_d, dt, count, _ptr(A), _ptr(D))
+    if rc != 0:
+        raise ValueError(f"orc_sample_bgpair rc={rc}")
+    return A, D
+
+
+def _rc_bursts(d):
+    arrs = {k: np.ascontiguousarray(d[k], dtype=t) for k, t in
+            [("start", np.int64), ("stop", np.int64), ("istart", np.int64), ("phCount", np.int32),
+             ("burst_ad", np.int64), ("burst_dd", np.int64), ("T", np.float32)]}
+    bs = OrcRcBursts(arrs["start"].size, _ptr(arrs["start"]), _ptr(arrs["stop"]), _ptr(arrs["istart"]),
+                     _ptr(arrs["phCount"]), _ptr(arrs["burst_ad"]), _ptr(arrs["burst_dd"]),
+                     _ptr(arrs["T"]), d["clk_p"], d["bg_ad_rate"], d["bg_dd_rate"])
+    return bs, arrs
+
+
+def rc_record(rc_data, n, args, m, R, seed, cap):
+    """The oracle's own Philox draws of every mc_kernel unit, in the tape
+    format: (tape[B*R, cap], tape_len[B*R], mcE[B*R])."""
+    bs, keep = _rc_bursts(rc_data)
+    units = bs.B * R
+    tape = np.zeros((units, cap), dtype=TAPE_DTYPE)
+    tlen = np.zeros(units, dtype=np.int32)
+    mcE = np.zeros(units, dtype=np.float32)
+    a = np.ascontiguousarray(args, dtype=np.float32)
+    rc = lib().orc_rc_record(C.byref(bs), n, _ptr(a), C.byref(m), R, seed, cap, _ptr(tape),
+                             _ptr(tlen), _ptr(mcE))
+    if rc != 0:
+        raise ValueError(f"orc_rc_record rc={rc}")
+    return tape, tlen, mcE
+
+
+def rc_replay(rc_data, n, args, m, R, tape, tape_len, ref_mcE):
+    """Replays recorded draws through the oracle's mc_kernel body. Returns
+    (mcE, status per unit, stats dict); status 0 = bit-exact with ref_mcE,
+    1 = differs, 2 = tape cut, 3 = draws out of order."""
+    bs, keep = _rc_bursts(rc_data)
+    units = bs.B * R
+    tape = np.ascontiguousarray(tape, dtype=TAPE_DTYPE).reshape(units, -1)
+    tl = np.ascontiguousarray(tape_len, dtype=np.int32)
+    ref = np.ascontiguousarray(ref_mcE, dtype=np.float32).reshape(-1)
+    out = np.zeros(units, dtype=np.float32)
+    status = np.zeros(units, dtype=np.int8)
+    st = OrcReplayStats()
+    a = np.ascontiguousarray(args, dtype=np.float32)
+    rc = lib().orc_rc_replay(C.byref(bs), n, _ptr(a), C.byref(m), R, _ptr(tape), _ptr(tl),
+                             tape.shape[1], _ptr(ref), _ptr(out), _ptr(status), C.byref(st))
+    if rc != 0:
+        raise ValueError(f"orc_rc_replay rc={rc}")
+    stats = {f: getattr(st, f) for f, _ in OrcReplayStats._fields_}
+    return out, status, stats
 
 
 def chi2(hist, ohist, nbins, left_pad, S, n_states):

@@ -200,3 +200,31 @@ def test_edge_cases(orc):
     args_sing, _ = static_args([0.1, 0.9], [0.0, 0.0])
     with pytest.raises(ValueError):
         orc.run_pda(N, T, 2, args_sing, m, 0, 4, 1)
+
+
+@pytest.mark.parametrize("lam", [0.5, 5.0, 9.9])
+@pytest.mark.parametrize("pa", [800.0 / 2300.0, 0.1])
+def test_background_pair_joint_law_is_two_independent_poissons(orc, lam, pa):
+    """The photon step's background pair (A, D) drawn from one uniform (the
+    total by inversion, then Bernoulli splits on the uniform's rescaled
+    residual; the GPU matches this mirror bit for bit) against independent
+    Poisson(lam pa) x Poisson(lam (1 - pa)): chi-square goodness of fit over
+    the joint table (cells with expectation below 5 lumped), 2e6 variates."""
+    from scipy import stats
+    la, ld = lam * pa, lam * (1.0 - pa)
+    A, D = orc.sample_bgpair(11, np.float32(la), np.float32(ld), 1.0, 2_000_000)
+    K = 40
+    obs = np.zeros((K, K))
+    np.add.at(obs, (np.minimum(A, K - 1), np.minimum(D, K - 1)), 1)
+    pmf_a = stats.poisson.pmf(np.arange(K), la)
+    pmf_a[-1] = stats.poisson.sf(K - 2, la)
+    pmf_d = stats.poisson.pmf(np.arange(K), ld)
+    pmf_d[-1] = stats.poisson.sf(K - 2, ld)
+    exp = np.outer(pmf_a, pmf_d) * A.size
+    keep = exp >= 5.0
+    o = np.append(obs[keep], obs[~keep].sum())
+    e = np.append(exp[keep], exp[~keep].sum())
+    chi = float(((o - e) ** 2 / e).sum())
+    p = stats.chi2.sf(chi, o.size - 1)
+    assert p > 1e-4, (chi, o.size - 1, p)
+    assert abs(np.corrcoef(A, D)[0, 1]) < 5e-3
