@@ -18,9 +18,18 @@ reads the 61.5 MB burst store from the pinned host arrays over the host link
 (each CTA checks its bursts, stages them and writes them through to the
 device store), and reads back histogram + chi-square.
 
+roofline: the dominant kernel (pda_kernel<1>) against the lane-operation rate
+(152 SMs x 128 lanes x the median SM clock sampled in the timed region), with
+the cost model of gsmfretda_gb300/roofline.py; its HBM side beside it.
+parity: the CPU oracle run at the seed of the last timed step, its histogram
+and chi-square compared with the GPU's. population_256 / fit_4state: short
+runs of the batched-population and time-to-fit workloads (their full runs:
+--workload population_256 / fit_4state).
+
 --impl reference times the CPU restatement of the path (the reference has no
-CPU Monte-Carlo of its own) on the host cores of this machine, all threads.
-N > 1 (torchrun): independent replicas, one per GPU, max-over-ranks timing.
+CPU Monte-Carlo of its own) on the host cores of this machine, all threads,
+on the same workload. N > 1 (torchrun): independent replicas, one per GPU,
+max-over-ranks timing.
 """
 import argparse
 import json
@@ -59,6 +68,11 @@ def parse():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="gpda", choices=["gpda", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the population_256 and fit_4state summaries of the default line")
+    ap.add_argument("--extra-pop-steps", type=int, default=5)
+    ap.add_argument("--extra-fit-gens", type=int, default=30)
+    ap.add_argument("--extra-fit-steps", type=int, default=150)
     ap.add_argument("--bursts", type=int, default=B_FULL)
     ap.add_argument("--fit-bursts", type=int, default=1_000_000)
     ap.add_argument("--fit-gens", type=int, default=80)
@@ -167,30 +181,42 @@ def cpu_threads():
         return os.cpu_count() or 1
 
 
-def oracle_rate(bs, n, args, md, S, b1, reps=1):
-    """Units/s of the CPU restatement (all host threads) on bursts [0, b1)."""
+def oracle_leg(bs, n, args, md, S, seed, gpu_hist, gpu_chi2, ohist, reps=2):
+    """Units/s of the CPU restatement (all host threads) on the full workload,
+    best of `reps` runs; the first run uses `seed`, and its histogram and
+    reduced chi-square are compared with the GPU's for the same seed."""
+    import numpy as np
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import build_oracle
     build_oracle.build()
     import orc
     m = orc.model(**md)
     th = cpu_threads()
-    best = 0.0
+    best, parity = 0.0, None
     for r in range(reps):
         t0 = time.perf_counter()
-        orc.run_pda(bs.N, bs.T, n, args, m, 1, S, 1000 + r, b0=0, b1=b1, off_idx=bs.off_idx,
-                    offsets=bs.offsets, nthreads=th)
+        h, _ = orc.run_pda(bs.N, bs.T, n, args, m, 1, S, seed + r, off_idx=bs.off_idx,
+                           offsets=bs.offsets, nthreads=th)
         dt = time.perf_counter() - t0
-        best = max(best, b1 * S / dt)
-    return best, th
+        best = max(best, bs.B * S / dt)
+        if r == 0:
+            c = orc.chi2(h[0], ohist, md["nbins"], md["left_pad"], S, n)
+            diff = np.nonzero(np.asarray(h[0], dtype=np.uint64) != np.asarray(gpu_hist, dtype=np.uint64))[0]
+            parity = {"hist": "bit-exact" if diff.size == 0 else f"first differing bin {int(diff[0])}",
+                      "chi2": "bit-exact" if float(c) == float(gpu_chi2) else f"{gpu_chi2!r} vs {c!r}",
+                      "seed": seed, "units": bs.B * S,
+                      "against": "oracle (CPU restatement), same Philox counters"}
+    return best, th, parity
 
 
 def run_reference(a):
+    """The CPU restatement of the path (the reference has no CPU Monte-Carlo
+    of its own) on the same workload as the GPU arm: every step simulates all
+    bursts x samples of photon_3state on all host threads."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
     bs, n, args, md, S = workload(a.bursts)
-    sample_b = min(20_000, bs.B)
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import build_oracle
     build_oracle.build()
@@ -198,21 +224,21 @@ def run_reference(a):
     m = orc.model(**md)
     th = cpu_threads()
     for w in range(a.warmup):
-        orc.run_pda(bs.N, bs.T, n, args, m, 1, S, 500 + w, b0=0, b1=sample_b, off_idx=bs.off_idx,
-                    offsets=bs.offsets, nthreads=th)
+        orc.run_pda(bs.N, bs.T, n, args, m, 1, S, 500 + w, off_idx=bs.off_idx, offsets=bs.offsets,
+                    nthreads=th)
     t0 = time.perf_counter()
     for k in range(a.steps):
-        orc.run_pda(bs.N, bs.T, n, args, m, 1, S, 900 + k, b0=0, b1=sample_b, off_idx=bs.off_idx,
-                    offsets=bs.offsets, nthreads=th)
+        orc.run_pda(bs.N, bs.T, n, args, m, 1, S, 900 + k, off_idx=bs.off_idx, offsets=bs.offsets,
+                    nthreads=th)
     dt = time.perf_counter() - t0
-    value = a.steps * sample_b * S / dt
-    sample = f"bursts [0,{sample_b}) of the workload x {S} samples per step"
+    value = a.steps * bs.B * S / dt
+    sample = f"full workload per step ({bs.B} bursts x {S} samples)"
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": a.gpus,
             "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 * dt / a.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded)",
-            "config": {"workload": WORKLOAD, "bursts": a.bursts, "samples": S, "states": n,
-                       "param_sets": 1, "mode": "photon-by-photon"},
+            "config": {"workload": WORKLOAD, "bursts": bs.B, "samples": S, "states": n,
+                       "param_sets": 1, "mode": "photon-by-photon", "photons": int(bs.off_idx[-1])},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": th, "kind": "port",
                              "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -220,21 +246,19 @@ def run_reference(a):
     return 0
 
 
-def run_population(a):
+def population_measure(local, steps, warmup, refflow=True):
     """Batched population (256 two-state parameter sets x 50,000 Pareto-N bursts
-    x 50 samples, occupancy mode) in one launch, against the plain path: one
-    launch + fetch per parameter set. Also times the reference's flow for a
-    parameter set (per-sample values read back, host histogram + chi-square,
+    x 50 samples, occupancy mode): the whole population in one captured graph
+    (tile autotuned first), against the plain path, gpda_run_plain: one
+    launch + read-back per parameter set. With refflow, also the reference's
+    flow for a parameter set (per-sample values read back, host histogram,
     src/mc.cu:567-587 + src/streamWorker.cpp:184-206) on the same kernel."""
     import numpy as np
     import torch
 
-    from gsmfretda_gb300 import build as gbuild
     from gsmfretda_gb300 import synth
-    gbuild.build()
     from gsmfretda_gb300.api import MODE_OCCUPANCY, Engine
 
-    local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
     bs, n, args, md, S = synth.population_256()
     P = args.shape[0]
@@ -244,26 +268,26 @@ def run_population(a):
     eng.set_observed(ohist.astype(np.float32))
     units = P * bs.B * S
     # launch-based batched step (one asynchronous launch per step)
-    for w in range(a.warmup):
+    for w in range(warmup):
         eng.launch(MODE_OCCUPANCY, n, args, S, 100 + w)
     eng.synchronize()
     t0 = time.perf_counter()
-    for k in range(a.steps):
+    for k in range(steps):
         eng.launch(MODE_OCCUPANCY, n, args, S, 200 + k)
     eng.fetch(P)
-    launch_s = (time.perf_counter() - t0) / a.steps
+    launch_s = (time.perf_counter() - t0) / steps
     # autotuned tile, then the whole step captured as one CUDA graph
     tile = eng.autotune(MODE_OCCUPANCY, n, args, S)
     eng.graph_create(MODE_OCCUPANCY, n, P, S)
-    for w in range(a.warmup):
+    for w in range(warmup):
         eng.graph_run(args, 100 + w)
     l0 = eng.launch_count
     t0 = time.perf_counter()
     kms = []
-    for k in range(a.steps):
+    for k in range(steps):
         hist, chi2 = eng.graph_run(args, 200 + k)
         kms.append(eng.lib.gpda_kernel_ms(eng.ctx))
-    batched_s = (time.perf_counter() - t0) / a.steps
+    batched_s = (time.perf_counter() - t0) / steps
     launches = eng.launch_count - l0
     # plain: one launch + fetch per parameter set
     eng.run_plain(MODE_OCCUPANCY, n, args[0], S, 1)
@@ -271,32 +295,45 @@ def run_population(a):
     for p in range(P):
         eng.run_plain(MODE_OCCUPANCY, n, args[p], S, 300 + p)
     plain_s = time.perf_counter() - t0
-    # reference flow for a few parameter sets: per-unit values to the host, host histogram
-    rp = 8
-    t0 = time.perf_counter()
-    for p in range(rp):
-        u, _ = eng.run_units(MODE_OCCUPANCY, n, args[p], S, 400 + p)
-        A = u[0].astype(np.int64)
-        Nb = np.repeat(bs.N.astype(np.int64), S).reshape(A.shape)
-        b = np.minimum(A * md["nbins"] // Nb, md["nbins"] - 1)
-        np.bincount(b.ravel(), minlength=md["nbins"])
-    refflow_s = (time.perf_counter() - t0) / rp * P
-    line = {"metric": METRIC, "value": units / batched_s, "unit": UNIT, "n_gpus": 1,
-            "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 * batched_s,
+    out = {"workload": "population_256", "param_sets": P, "bursts": bs.B, "samples": S,
+           "tile_bursts": tile, "batched_value": units / batched_s,
+           "batched_ms_per_step": 1e3 * batched_s, "kernel_ms": sum(kms) / len(kms),
+           "launch_value": units / launch_s, "plain_value": units / plain_s,
+           "plain_ms_per_population": 1e3 * plain_s,
+           "batched_over_plain": plain_s / batched_s, "gate": ">= 20x gpda_run_plain",
+           "gpu_launches": int(launches),
+           "chi2_min": float(np.min(chi2)), "chi2_argmin": int(np.argmin(chi2))}
+    if refflow:
+        rp = 8
+        t0 = time.perf_counter()
+        for p in range(rp):
+            u, _ = eng.run_units(MODE_OCCUPANCY, n, args[p], S, 400 + p)
+            A = u[0].astype(np.int64)
+            Nb = np.repeat(bs.N.astype(np.int64), S).reshape(A.shape)
+            b = np.minimum(A * md["nbins"] // Nb, md["nbins"] - 1)
+            np.bincount(b.ravel(), minlength=md["nbins"])
+        refflow_s = (time.perf_counter() - t0) / rp * P
+        out["refflow_value"] = units / refflow_s
+        out["batched_over_refflow"] = refflow_s / batched_s
+    eng.close()
+    return out
+
+
+def run_population(a):
+    from gsmfretda_gb300 import build as gbuild
+    gbuild.build()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    r = population_measure(local, a.steps, a.warmup)
+    line = {"metric": METRIC, "value": r["batched_value"], "unit": UNIT, "n_gpus": 1,
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": r["batched_ms_per_step"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded)",
-            "config": {"workload": "population_256", "bursts": bs.B, "samples": S, "states": n,
-                       "param_sets": P, "mode": "occupancy", "graph": True, "tile_bursts": tile},
-            "gpu_launches": int(launches),
-            "kernel_ms": sum(kms) / len(kms),
-            "launch_value": units / launch_s,
-            "plain_value": units / plain_s,
-            "batched_over_plain": plain_s / batched_s,
-            "refflow_value": units / refflow_s,
-            "batched_over_refflow": refflow_s / batched_s,
-            "chi2_min": float(np.min(chi2)), "chi2_argmin": int(np.argmin(chi2))}
+            "config": {"workload": "population_256", "bursts": r["bursts"], "samples": r["samples"],
+                       "states": 2, "param_sets": r["param_sets"], "mode": "occupancy",
+                       "graph": True, "tile_bursts": r["tile_bursts"]},
+            "gpu_launches": r["gpu_launches"]}
+    line.update({k: v for k, v in r.items() if k not in ("workload", "gpu_launches")})
     print(json.dumps(line), flush=True)
-    eng.close()
     return 0
 
 
@@ -398,10 +435,10 @@ def run_expected(a):
     return 0
 
 
-def run_fit(a):
+def fit_measure(local, bursts, gens, adam_steps, with_batched=True, clocks=None):
     """Time-to-fit on the 4-state cyclic system (8 nonzero rates, E = 0.15,
-    0.4, 0.6, 0.9) with 1,000,000 Pareto-N bursts (alpha 1.8, 30-3000
-    photons, T lognormal around 2 ms): the observed histogram is one sampled
+    0.4, 0.6, 0.9) with Pareto-N bursts (alpha 1.8, 30-3000 photons, T
+    lognormal around 2 ms), 41 bins: the observed histogram is one sampled
     draw per burst at the true parameters; every fit starts from the same
     perturbed point.
       es_plain    separable CMA-ES, population 64, sampled chi-square (10 MC
@@ -416,14 +453,11 @@ def run_fit(a):
     import numpy as np
     import torch
 
-    from gsmfretda_gb300 import build as gbuild
     from gsmfretda_gb300 import fit, synth
-    gbuild.build()
     from gsmfretda_gb300.api import MODE_OCCUPANCY, Engine
 
-    local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
-    bs, n, truth, md, _ = synth.fit_4state(B=a.fit_bursts)
+    bs, n, truth, md, _ = synth.fit_4state(B=bursts)
     # 21 bins leave 19 - n(n+1) = -1 degrees of freedom in the reduced chi-square
     md = dict(md, nbins=41)
     eng = Engine(local, **md)
@@ -442,18 +476,17 @@ def run_fit(a):
     prob.expected(z0, 16, 1)
     prob.sampled_batched(np.stack([z0] * 64), 10, 1)
     prob.sampled_plain(z0[None], 10, 1)
-    clocks = ClockSampler(local)
-    clocks.start()
     runs = {}
-    clocks.mark()
+    if clocks:
+        clocks.mark()
     runs["es_plain"] = fit.sep_cma_es(prob, z0, 0.3, 64, prob.sampled_plain, 10, seed=11,
-                                      generations=a.fit_gens)
-    runs["es_batched"] = fit.sep_cma_es(prob, z0, 0.3, 64, prob.sampled_batched, 10, seed=11,
-                                        generations=a.fit_gens)
-    runs["adam"] = fit.adam(prob, z0, steps=a.fit_steps, lr=0.05, samples=16, seed=5)
-    clocks.mark()
-    time.sleep(0.2)
-    clocks.stop()
+                                      generations=gens)
+    if with_batched:
+        runs["es_batched"] = fit.sep_cma_es(prob, z0, 0.3, 64, prob.sampled_batched, 10, seed=11,
+                                            generations=gens)
+    runs["adam"] = fit.adam(prob, z0, steps=adam_steps, lr=0.05, samples=16, seed=5)
+    if clocks:
+        clocks.mark()
     curves = {k: [yard(z) for z in r.best_z] for k, r in runs.items()}
     y_true, y0 = yard(z_true), yard(z0)
     target = curves["es_plain"][-1]
@@ -471,20 +504,40 @@ def run_fit(a):
                   "best_chi2": min(curves[k])}
     base = out["es_plain"]["time_to_target_s"]
     adam_t = out["adam"]["time_to_target_s"]
-    line = {"metric": "time-to-fit at fixed chi-square", "value": adam_t, "unit": "s",
-            "n_gpus": 1, "steps": a.fit_steps, "warmup": 1, "ms_per_step": 1e3 * out["adam"]["total_s"] / out["adam"]["iterations"],
+    res = {"workload": "fit_4state", "bursts": bs.B, "states": n, "free_rates": int(prob.free.size),
+           "nbins": md["nbins"], "es_population": 64, "es_samples": 10, "es_generations": gens,
+           "adam_steps": adam_steps, "adam_samples": 16, "adam_lr": 0.05,
+           "yardstick": "expected chi2, 32 samples, seed 0x5EED",
+           "target_chi2": target, "chi2_true": y_true, "chi2_start": y0,
+           "adam_time_to_target_s": adam_t, "es_plain_time_to_target_s": base,
+           "speedup_vs_es_plain": (base / adam_t) if (base and adam_t) else None,
+           "runs": out, "fitted_E": [float(x) for x in prob.to_args(runs["adam"].z)[0][:n]]}
+    eng.close()
+    return res
+
+
+def run_fit(a):
+    from gsmfretda_gb300 import build as gbuild
+    gbuild.build()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    clocks = ClockSampler(local)
+    clocks.start()
+    r = fit_measure(local, a.fit_bursts, a.fit_gens, a.fit_steps, with_batched=True, clocks=clocks)
+    time.sleep(0.2)
+    clocks.stop()
+    adam = r["runs"]["adam"]
+    line = {"metric": "time-to-fit at fixed chi-square", "value": r["adam_time_to_target_s"],
+            "unit": "s", "n_gpus": 1, "steps": a.fit_steps, "warmup": 1,
+            "ms_per_step": 1e3 * adam["total_s"] / adam["iterations"],
             "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32 masses / f64 chi-square", "data": "synthetic (seeded)",
-            "config": {"workload": "fit_4state", "bursts": bs.B, "states": n, "free_rates": int(prob.free.size),
-                       "nbins": md["nbins"],
-                       "es_population": 64, "es_samples": 10, "es_generations": a.fit_gens,
-                       "adam_samples": 16, "adam_lr": 0.05, "yardstick": "expected chi2, 32 samples, seed 0x5EED"},
-            "target_chi2": target, "chi2_true": y_true, "chi2_start": y0,
-            "speedup_vs_es_plain": (base / adam_t) if (base and adam_t) else None,
-            "runs": out, "clocks": clocks.summary(),
-            "fitted_E": [float(x) for x in prob.to_args(runs["adam"].z)[0][:n]]}
+            "config": {k: r[k] for k in ("workload", "bursts", "states", "free_rates", "nbins",
+                                         "es_population", "es_samples", "es_generations",
+                                         "adam_samples", "adam_lr", "yardstick")},
+            "clocks": clocks.summary()}
+    line.update({k: r[k] for k in ("target_chi2", "chi2_true", "chi2_start", "speedup_vs_es_plain",
+                                   "runs", "fitted_E")})
     print(json.dumps(line), flush=True)
-    eng.close()
     return 0
 
 
@@ -594,17 +647,21 @@ def main():
     h2d = hN.nbytes + hT.nbytes + hOI.nbytes + hOF.nbytes + hA.nbytes
     d2h = 8 * md["nbins"] + 8 + 4
 
-    # ---------------- roofline of the dominant kernel (HBM side; the path is ALU bound)
+    # ---------------- roofline of the dominant kernel: the lane-operation
+    # rate (the path is ALU bound); the HBM figures beside it
     kavg_ms = sum(kern_ms) / len(kern_ms)
     alg_bytes = 4 * bs.B + 4 * bs.B + 8 * (bs.B + 1) + 4 * int(bs.off_idx[-1])
     hbm_peak, peak_kind, sm_max = peaks()
     achieved_gbs = alg_bytes / (kavg_ms * 1e-3) / 1e9
     from gsmfretda_gb300 import roofline as rl
-    ops_per_unit, segs = rl.photon_ops_per_unit(n, args, bs.N, bs.T)
-    alu_peak = rl.lane_peak_gops(sm_max)               # FP32/INT32 lane-ops per s, in Gop/s
-    alu_achieved = units / (kavg_ms * 1e-3) * ops_per_unit / 1e9
-    alu_issued = units / (kavg_ms * 1e-3) * ISSUED_INST_PER_UNIT / 1e9
-
+    cost = rl.photon_ops_breakdown(n, args, bs.N, bs.T)
+    clk = clocks.summary()
+    sm_mhz = clk.get("sm_mhz") or sm_max
+    alu_peak = rl.lane_peak_gops(sm_mhz)               # FP32/INT32 lane-ops per s, in Gop/s
+    unit_rate = units / (kavg_ms * 1e-3)
+    alu_achieved = unit_rate * cost["ops"] / 1e9
+    alu_issued = unit_rate * ISSUED_INST_PER_UNIT / 1e9
+    traffic = NCU_TRAFFIC_BYTES if bs.B == B_FULL else None
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": 1e3 * total_s / a.steps, "higher_is_better": True,
@@ -616,28 +673,57 @@ def main():
         "e2e": {"value": world * units / e2e_mean, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(launches),
-        "clocks": clocks.summary(),
-        "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved_gbs / hbm_peak,
-                     "traffic": NCU_TRAFFIC_BYTES if bs.B == B_FULL else None, "peak_kind": peak_kind,
-                     "algorithmic_bytes_per_launch": alg_bytes, "kernel_ms": kavg_ms,
-                     "alu": {"achieved": alu_achieved, "peak": alu_peak, "unit": "Gop/s",
-                             "frac": alu_achieved / alu_peak, "ops_per_unit": ops_per_unit,
-                             "segments_per_unit": segs,
-                             "issued": alu_issued, "issued_frac": alu_issued / alu_peak,
-                             "issued_inst_per_unit": ISSUED_INST_PER_UNIT,
-                             "what": "algorithmic ops (cost model of gsmfretda_gb300/roofline.py "
-                                     "on this workload) and issued thread instructions (ncu) vs "
-                                     "152 SMs x 128 lanes x SM clock"}},
+        "clocks": clk,
+        "roofline": {
+            "bound": "alu", "achieved": alu_achieved, "peak": alu_peak, "unit": "Gop/s",
+            "frac": alu_achieved / alu_peak, "traffic": traffic,
+            "peak_kind": f"lane-issue rate, 152 SMs x 128 lanes x {sm_mhz:.0f} MHz (median SM clock "
+                         "sampled in the timed region); MEASURED_PEAKS.json holds no ALU peak",
+            "kernel": "pda_kernel<1>", "kernel_ms": kavg_ms,
+            "ops_per_unit": cost["ops"],
+            "cost_model": {"draws": cost["draws"], "search": cost["search"],
+                           "segments_per_unit": cost["segments"], "mean_photons": cost["mean_photons"],
+                           "linear_scan_not_counted": cost["linear_scan"],
+                           "frac_if_linear_scan_counted": unit_rate * (cost["draws"] + cost["linear_scan"])
+                           / 1e9 / alu_peak,
+                           "source": "gsmfretda_gb300/roofline.py"},
+            "issued": {"inst_per_unit": ISSUED_INST_PER_UNIT, "achieved": alu_issued,
+                       "frac": alu_issued / alu_peak,
+                       "source": "ncu thread instructions per unit, profiles/pda_kernel_photon_3state.txt"},
+            "hbm": {"achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
+                    "frac": achieved_gbs / hbm_peak, "peak_kind": peak_kind,
+                    "algorithmic_bytes_per_launch": alg_bytes, "traffic": traffic}},
         "chi2_last": float(chi2[0]),
     }
     if rank == 0 and world == 1 and not a.no_cpu_baseline:
-        rate, th = oracle_rate(bs, n, args, md, S, bs.B, reps=2)
+        # the oracle on the full workload at the seed of the last timed step:
+        # timed as the CPU baseline, and compared with that step's histogram
+        # and chi-square
+        rate, th, parity = oracle_leg(bs, n, args, md, S, 20_000 + a.steps - 1, hist[0], chi2[0],
+                                      ohist.astype(np.float32))
         line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": th, "kind": "port",
                                 "sample": f"full workload ({bs.B} bursts x {S} samples), best of 2"}
+        line["parity"] = parity
+    if rank == 0 and world == 1 and not a.no_extras:
+        eng.close()
+        eng = None
+        pop = population_measure(local, a.extra_pop_steps, 2, refflow=False)
+        line["population_256"] = {k: pop[k] for k in (
+            "param_sets", "bursts", "samples", "tile_bursts", "batched_value", "plain_value",
+            "batched_over_plain", "kernel_ms", "batched_ms_per_step", "plain_ms_per_population",
+            "gate")}
+        line["population_256"]["steps"] = a.extra_pop_steps
+        fr = fit_measure(local, 1_000_000, a.extra_fit_gens, a.extra_fit_steps, with_batched=False)
+        line["fit_4state"] = {k: fr[k] for k in (
+            "bursts", "nbins", "es_generations", "adam_steps", "target_chi2", "chi2_true",
+            "adam_time_to_target_s", "es_plain_time_to_target_s", "speedup_vs_es_plain", "fitted_E")}
+        line["fit_4state"]["reduced"] = (f"{a.extra_fit_gens} evolutionary generations and "
+                                         f"{a.extra_fit_steps} Adam steps (full run: bench.py "
+                                         "--workload fit_4state)")
     if rank == 0:
         print(json.dumps(line), flush=True)
-    eng.close()
+    if eng is not None:
+        eng.close()
     if dist:
         dist.destroy_process_group()
     return 0

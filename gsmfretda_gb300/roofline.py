@@ -8,14 +8,21 @@ counted with fixed costs per operation:
     PHILOX_WORD     25  INT32 ops per 32-bit Philox4x32-10 word (~100 per block)
     LOG             16  FP32 ops per logarithm (one per dwell)
     BINOMIAL        40  ops per binomial draw (BTRD, or a table inversion)
-    PHOTON_COMPARE   2  ops per photon assigned to a segment (photon mode)
+    SEARCH_STEP      4  ops per bisection step over a burst's sorted arrival
+                        offsets (midpoint, load, compare, select)
 
 and the draws of the photon-by-photon model: with D dwell segments per unit,
 1 + 2D + 4 + D random words (initial state; jump and dwell per segment;
-background; one binomial per segment), D logarithms and D binomials, and every
-photon compared once:
+background; one binomial per segment), D logarithms and D binomials, and one
+bisection of the burst's N sorted offsets per segment that ends inside the
+burst (the last segment takes the photons left):
 
-    ops(D, N) = PHILOX_WORD (5 + 3 D) + (LOG + BINOMIAL) D + PHOTON_COMPARE N.
+    ops(D, N) = PHILOX_WORD (5 + 3 D) + (LOG + BINOMIAL) D
+                + SEARCH_STEP (D - 1) log2(N + 1).
+
+A linear scan that compares every photon once (PHOTON_COMPARE = 2 ops per
+photon, 2 N per unit) is the other way to assign photons; it is reported
+beside the model for comparison, not counted: the kernels bisect.
 
 D is computed from the workload, not assumed: a trajectory started from the
 stationary law pi of the rate matrix K jumps at the stationary flux
@@ -27,6 +34,7 @@ import numpy as np
 PHILOX_WORD = 25
 LOG = 16
 BINOMIAL = 40
+SEARCH_STEP = 4
 PHOTON_COMPARE = 2
 
 
@@ -63,13 +71,24 @@ def mean_segments(n, args, T):
     return 1.0 + flux * float(np.mean(np.asarray(T, dtype=np.float64)))
 
 
+def photon_ops_breakdown(n, args, N, T):
+    """The cost model's terms per unit on bursts with photon counts N and
+    durations T: draws (Philox words, logarithms, binomials), search (the
+    bisections that assign photons to segments), their sum, the linear-scan
+    alternative (not counted) and D."""
+    D = mean_segments(n, args, T)
+    Nbar = float(np.mean(np.asarray(N, dtype=np.float64)))
+    draws = PHILOX_WORD * (5.0 + 3.0 * D) + (LOG + BINOMIAL) * D
+    search = SEARCH_STEP * (D - 1.0) * float(np.log2(Nbar + 1.0))
+    return {"draws": draws, "search": search, "ops": draws + search,
+            "linear_scan": PHOTON_COMPARE * Nbar, "segments": D, "mean_photons": Nbar}
+
+
 def photon_ops_per_unit(n, args, N, T):
     """(ops per unit, D) of the photon-by-photon model on bursts with photon
     counts N and durations T."""
-    D = mean_segments(n, args, T)
-    Nbar = float(np.mean(np.asarray(N, dtype=np.float64)))
-    ops = PHILOX_WORD * (5.0 + 3.0 * D) + (LOG + BINOMIAL) * D + PHOTON_COMPARE * Nbar
-    return ops, D
+    b = photon_ops_breakdown(n, args, N, T)
+    return b["ops"], b["segments"]
 
 
 def lane_peak_gops(sm_mhz, sms=152, lanes=128):

@@ -50,6 +50,10 @@ def test_mean_segments_match_a_direct_simulation():
 def test_photon_ops_per_unit_formula():
     bs, n, args, md, S = synth.photon_3state(B=2000, seed=2)
     ops, D = rl.photon_ops_per_unit(n, args, bs.N, bs.T)
-    expect = 25 * (5 + 3 * D) + 56 * D + 2 * float(np.mean(bs.N))
+    Nbar = float(np.mean(bs.N))
+    expect = 25 * (5 + 3 * D) + 56 * D + 4 * (D - 1) * np.log2(Nbar + 1)
     assert abs(ops - expect) < 1e-9
+    b = rl.photon_ops_breakdown(n, args, bs.N, bs.T)
+    assert abs(b["draws"] + b["search"] - ops) < 1e-9
+    assert abs(b["linear_scan"] - 2 * Nbar) < 1e-9
 
