@@ -158,6 +158,13 @@ def max_over_ranks(x, dist, device=None):
     return float(t.item())
 
 
+def replica_value(units_per_rank, steps, total_s, world):
+    """Whole-job throughput of `world` replicas that each process
+    units_per_rank units per step for `steps` steps; total_s is the slowest
+    rank's time (max over ranks)."""
+    return world * units_per_rank * steps / total_s
+
+
 def workload(B):
     from gsmfretda_gb300 import synth
     bs, n, args, md, S = synth.photon_3state(B=B, seed=2)
@@ -623,7 +630,7 @@ def main():
     time.sleep(0.2)
     clocks.stop()
     total_s = max_over_ranks(total_s, dist, device=f"cuda:{local}")
-    value = world * units * a.steps / total_s
+    value = replica_value(units, a.steps, total_s, world)
 
     # ---------------- end to end through the C ABI with pinned host buffers
     pin = lambda x, dt: torch.from_numpy(np.ascontiguousarray(x, dtype=dt)).pin_memory().numpy()  # noqa: E731
