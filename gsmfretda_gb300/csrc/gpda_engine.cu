@@ -106,7 +106,10 @@ struct gpda_ctx {
 
 namespace {
 
-constexpr int kSmemCapFloats = 8192;  // photon staging: 32 KB of dynamic shared memory
+#ifndef GPDA_SMEM_CAP
+#define GPDA_SMEM_CAP 8192
+#endif
+constexpr int kSmemCapFloats = GPDA_SMEM_CAP;  // photon staging (dynamic shared memory, floats)
 constexpr int kMaxRanges = 64;        // burst ranges of gpda_run_host
 constexpr int kRangeStreams = 4;      // streams its range kernels are spread over
 constexpr int kFusedCheckSets = 4;    // photon run_host: CTAs check the store up to this P
@@ -183,12 +186,22 @@ int ensure_scratch(gpda_ctx *c, int P) {
 // units. Photon mode keeps its tiles: there a lane takes the tile's next unit
 // as soon as its own is done, and tiles of fewer units per lane measured
 // slower than the end-of-launch imbalance they remove.
+#ifndef GPDA_TILE_UNITS
+#define GPDA_TILE_UNITS 2048
+#endif
+#ifndef GPDA_TAIL_DIV
+#define GPDA_TAIL_DIV 0
+#endif
+#ifndef GPDA_TAIL_WAVES
+#define GPDA_TAIL_WAVES 1
+#endif
+
 int tile_bursts(const gpda_ctx *c, int mode, int S, int64_t nb, int P) {
     int tb = 0;
     for (const auto &t : c->tuned)
         if (t[0] == mode && t[1] == S) tb = t[2];
     if (tb == 0) {
-        tb = (2048 + S - 1) / S;
+        tb = (GPDA_TILE_UNITS + S - 1) / S;
         if (mode == GPDA_MODE_PHOTON && c->mean_N > 0.0) {
             int fit = (int)(0.6 * kSmemCapFloats / c->mean_N);
             tb = std::min(tb, std::max(fit, 1));
@@ -293,6 +306,26 @@ int range_args(gpda_ctx *c, int mode, int P, int n, int64_t b0, int64_t b1, int 
     }
     a.abort_flag = abort_flag;
     grid = (int)std::min<int64_t>(a.n_items, (int64_t)c->num_sms * c->blocks_per_sm[mode]);
+#if GPDA_TAIL_DIV > 0
+    // photon mode: the last ~GPDA_TAIL_WAVES items' worth of bursts per CTA
+    // in tiles GPDA_TAIL_DIV times smaller, handed out last
+    if (mode == GPDA_MODE_PHOTON && a.tile_b >= 2 * GPDA_TAIL_DIV) {
+        const int64_t nb_all = b1 - b0;
+        const int ts = a.tile_b / GPDA_TAIL_DIV;
+        const int64_t tail = ((int64_t)grid * a.tile_b * GPDA_TAIL_WAVES + P - 1) / P;
+        if (tail < nb_all) {
+            const int64_t nbig = (nb_all - tail) / a.tile_b;
+            const int64_t nsmall = (nb_all - nbig * a.tile_b + ts - 1) / ts;
+            if ((nbig + nsmall) * P <= (int64_t)INT32_MAX && nbig > 0) {
+                a.tile_s = ts;
+                a.nbig = (int)nbig;
+                a.nsmall = (int)nsmall;
+                a.n_items = (int)((nbig + nsmall) * P);
+                grid = (int)std::min<int64_t>(a.n_items, (int64_t)c->num_sms * c->blocks_per_sm[mode]);
+            }
+        }
+    }
+#endif
     return GPDA_OK;
 }
 
@@ -606,6 +639,9 @@ gpda_ctx *gpda_create(int32_t device, const gpda_model *m, int32_t *status) {
     if (bad(cudaEventCreate(&c->k1))) return nullptr;
     if (bad(cudaEventRecord(c->params_ev, c->stream))) return nullptr;
     if (bad(pda_occupancy_blocks(0, 0, &c->blocks_per_sm[0]))) return nullptr;
+    // the photon kernels' staging may take them past the 48 KB default
+    if (bad(pda_set_smem_limit(1, sizeof(float) * kSmemCapFloats))) return nullptr;
+    if (bad(pda_set_smem_limit(kModePhotonDirect, sizeof(float) * kSmemCapFloats))) return nullptr;
     if (bad(pda_occupancy_blocks(1, sizeof(float) * kSmemCapFloats, &c->blocks_per_sm[1]))) return nullptr;
     if (bad(pda_occupancy_blocks(kModePhotonDirect, sizeof(float) * kSmemCapFloats,
                                  &c->blocks_per_sm[kModePhotonDirect]))) return nullptr;

@@ -74,7 +74,12 @@ struct PdaArgs {
     int32_t S;
     int32_t tile_b;               // bursts per work item
     int32_t ntiles;
-    int32_t n_items;              // ntiles * P
+    int32_t n_items;              // ntiles * P, or P * (nbig + nsmall)
+    // tile_s > 0: the range ends in smaller work items, handed out last: the
+    // first nbig tiles of tile_b bursts of every parameter set, then nsmall
+    // tiles of tile_s bursts of every parameter set (a shorter tail when the
+    // last items finish); tile_s = 0: ntiles tiles of tile_b bursts
+    int32_t nbig, nsmall, tile_s;
     int32_t nbins;
     int32_t smem_cap;             // photon staging capacity (floats)
     uint32_t pbase;               // parameter-set word of the counter = pbase + p

@@ -66,6 +66,25 @@ __device__ __forceinline__ Divisor sdiv(const uint32_t &m, const uint32_t &l) {
     return Divisor{*(const volatile uint32_t *)&m, *(const volatile uint32_t *)&l};
 }
 
+// The proximity-ratio bin min(A nbins / N, nbins - 1) of A acceptor photons
+// out of N (0 <= A <= N <= 2^21, nbins <= 1024), exact. x = A nbins < 2^31;
+// the float quotient (x rounded to float, then the approximate division,
+// relative error below 2^-21 in all) is within 5e-4 of x / N <= 1024, so its
+// truncation v is floor(x / N) or one off, and one integer comparison each
+// way corrects it (v N <= 1025 * 2^21 < 2^32).
+#ifndef GPDA_PR_BIN
+#define GPDA_PR_BIN 1
+#endif
+__device__ __forceinline__ int pr_bin(int A, int N, int nbins) {
+    const uint32_t x = (uint32_t)A * (uint32_t)nbins;
+    const uint32_t n = (uint32_t)N;
+    uint32_t v = __float2uint_rz(__fdividef((float)x, (float)N));
+    const uint32_t vn = v * n;
+    if (vn > x) v -= 1u;
+    else if (x - vn >= n) v += 1u;
+    return v >= (uint32_t)nbins ? nbins - 1 : (int)v;
+}
+
 // number of offsets < x in the sorted range a[lo, hi)
 __device__ __forceinline__ int lower_bound(const float *a, int lo, int hi, float x) {
     while (lo < hi) {
@@ -351,10 +370,20 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) pda_kernel(const PdaArgs
         __syncthreads();
         const int item = s_item;
         if (item >= a.n_items) break;
-        const int p = item / a.ntiles;
-        const int tile = item - p * a.ntiles;
-        const int64_t tb0 = a.b0 + (int64_t)tile * a.tile_b;
-        const int nb = (int)min((int64_t)a.tile_b, a.b1 - tb0);
+        int p;
+        int64_t tb0;
+        int nb;
+        if (a.tile_s == 0 || item < a.P * a.nbig) {
+            const int per = a.tile_s ? a.nbig : a.ntiles;
+            p = item / per;
+            tb0 = a.b0 + (int64_t)(item - p * per) * a.tile_b;
+            nb = (int)min((int64_t)a.tile_b, a.b1 - tb0);
+        } else {
+            const int j = item - a.P * a.nbig;
+            p = j / a.nsmall;
+            tb0 = a.b0 + (int64_t)a.nbig * a.tile_b + (int64_t)(j - p * a.nsmall) * a.tile_s;
+            nb = (int)min((int64_t)a.tile_s, a.b1 - tb0);
+        }
         {
             const uint32_t *src = reinterpret_cast<const uint32_t *>(a.params + p);
             uint32_t *dst = reinterpret_cast<uint32_t *>(&sp);
@@ -377,9 +406,10 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) pda_kernel(const PdaArgs
             }
             __syncthreads();
         }
-        // the bursts' divisors for binning (each thread reads the sN entries
-        // it wrote itself; the simulation reads them after a barrier)
-        for (int i = tid; i < nb; i += kThreads) {
+        // occupancy mode (and photon mode without pr_bin): the bursts'
+        // divisors for binning (each thread reads the sN entries it wrote
+        // itself; the simulation reads them after a barrier)
+        for (int i = tid; (!kPhoton || !GPDA_PR_BIN) && i < nb; i += kThreads) {
             const int32_t n_ = sN[i];
             const Divisor d = divisor_of(n_ > 0 ? (uint32_t)n_ : 1u);
             sNm[i] = d.m;
@@ -623,10 +653,14 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) pda_kernel(const PdaArgs
                     const int64_t b = tb0 + U.lb;
                     if (a.unit_out) a.unit_out[((int64_t)p * (a.b1 - a.b0) + (b - a.b0)) * a.S + U.s] = U.A;
                     if (U.Nb > 0 && U.A >= 0) {
+#if GPDA_PR_BIN
+                        bin = pr_bin(U.A, U.Nb, a.nbins);
+#else
                         // a hardware division here: the shared divisors cost this
                         // loop a register spill
                         unsigned v = (unsigned)U.A * (unsigned)a.nbins / (unsigned)U.Nb;
                         bin = v >= (unsigned)a.nbins ? a.nbins - 1 : (int)v;
+#endif
                     }
                 }
             }
