@@ -691,6 +691,225 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) pda_kernel(const PdaArgs
     if (a.chi2) last_cta_chi2(a);
 }
 
+// ---------------------------------------------------------------- photon mode, warp pipelines
+// pda_photon_warp_kernel: the photon-mode simulation without the end-of-item
+// idling of pda_kernel<1>. There all 256 threads share one staged tile, and a
+// lane whose units are done waits for the slowest unit of the tile before the
+// CTA stages the next one (about a fifth of the lane-steps at 21-burst tiles).
+// Here every warp pulls its own work items (w_tile bursts of one parameter
+// set) and keeps two in shared memory: while its lanes take units from one,
+// the other is refilled as soon as its last unit is done, its arrival offsets
+// copied with cp.async, so a lane whose unit ends takes the next unit at once,
+// from whichever item has one. Everything a warp shares lives in its own two
+// slots and is decided by warp votes: no CTA barrier in the simulation loop.
+// Units, counters and results are those of pda_kernel<1> (a unit's draws
+// depend only on its (parameter set, burst, sample)). Parameter sets live in
+// shared memory (P <= kWarpParSets), the histogram too (P nbins <= kHistBins).
+struct WarpSlot {
+    int64_t tb0;
+    int32_t p, nb, units, staged;
+    int32_t sN[kWarpTileMax];
+    float sT[kWarpTileMax];
+    int32_t sOff[kWarpTileMax + 1];
+};
+
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem, int src_bytes) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(sa), "l"(gmem), "r"(src_bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// The next work item of the launch for this warp (lane 0 claims, all lanes
+// get it); -1 when none is left.
+__device__ __forceinline__ int warp_claim(const PdaArgs &a, int lane) {
+    int it = 0;
+    if (lane == 0) it = (int)atomicAdd(a.work, 1u);
+    it = __shfl_sync(0xffffffffu, it, 0);
+    return it < a.w_items ? it : -1;
+}
+
+// Stage work item `item` into slot S (offsets into ph, cap floats): the
+// bursts' counts, durations and offset starts now; the offsets' 16-byte
+// span with cp.async (committed, not waited for). Whole warp.
+__device__ __forceinline__ void warp_stage(WarpSlot &S, float *ph, const PdaArgs &a, int item, int lane) {
+    const int p = item / a.w_ntiles;
+    const int64_t tb0 = a.b0 + (int64_t)(item - p * a.w_ntiles) * a.w_tile;
+    const int nb = (int)min((int64_t)a.w_tile, a.b1 - tb0);
+    int64_t oi = 0;
+    if (lane <= nb) oi = a.off_idx[tb0 + lane];
+    if (lane < nb) {
+        S.sN[lane] = a.N[tb0 + lane];
+        S.sT[lane] = a.T[tb0 + lane];
+    }
+    const int64_t first = __shfl_sync(0xffffffffu, oi, 0);
+    const int64_t last = __shfl_sync(0xffffffffu, oi, nb);
+    const int64_t abase = first & ~(int64_t)3;
+    const int64_t aend = (last + 3) & ~(int64_t)3;
+    const bool staged = (aend - abase) <= (int64_t)kWarpSlotFloats;
+    if (staged) {
+        if (lane <= nb) S.sOff[lane] = (int32_t)(oi - abase);
+        const int nv = (int)((aend - abase) >> 2);
+        // a caller's exactly sized array (exact_offsets) ends at a photon of
+        // some tile: the vector holding the tile's last photon is copied in
+        // part and zero-filled (no burst of this tile reads past it)
+        const int64_t vend = a.exact_offsets ? last : INT64_MAX;
+        for (int i = lane; i < nv; i += 32) {
+            const int64_t e = abase + 4 * (int64_t)i;
+            const int64_t rem = vend - e;
+            const int bytes = rem >= 4 ? 16 : (rem > 0 ? (int)rem * 4 : 0);
+            cp_async16(ph + 4 * i, a.offsets + (bytes > 0 ? e : abase), bytes);
+        }
+    }
+    cp_async_commit();
+    if (lane == 0) {
+        S.tb0 = tb0;
+        S.p = p;
+        S.nb = nb;
+        S.units = nb * a.S;
+        S.staged = staged ? 1 : 0;
+    }
+    __syncwarp();
+}
+
+__global__ void __launch_bounds__(kThreads, kMinBlocks) pda_photon_warp_kernel(const PdaArgs a) {
+    extern __shared__ float4 s_wph4[];
+    constexpr int kWarps = kThreads / 32;
+    __shared__ WarpSlot s_slot[kWarps][2];
+    __shared__ DevParams s_par[kWarpParSets];
+    __shared__ unsigned int sh[kHistBins];           // [p][bin]
+    __shared__ float s_inv[kInvTable];
+    __shared__ float s_bgc[4];
+    __shared__ uint32_t s_Sm, s_Sl;
+    __shared__ int s_abort;
+    const int tid = threadIdx.x;
+    const int lane = tid & 31;
+    const int w = tid >> 5;
+    if (tid == 0) {
+        s_abort = (a.abort_flag && __ldcg(a.abort_flag) != 0u) ? 1 : 0;
+        const Divisor dS = divisor_of((uint32_t)a.S);
+        s_Sm = dS.m;
+        s_Sl = dS.l;
+        const float bgs = a.bg_a + a.bg_d;
+        const float pa = a.bg_a / bgs;
+        s_bgc[0] = bgs;
+        s_bgc[1] = pa;
+        s_bgc[2] = 1.0f / pa;
+        s_bgc[3] = 1.0f / (1.0f - pa);
+    }
+    if (tid < kInvTable) s_inv[tid] = tid > 0 ? 1.0f / (float)tid : 0.0f;
+    for (int i = tid; i < a.P * kParamWords; i += kThreads)
+        reinterpret_cast<uint32_t *>(s_par)[i] = reinterpret_cast<const uint32_t *>(a.params)[i];
+    for (int i = tid; i < a.P * a.nbins; i += kThreads) sh[i] = 0u;
+    __syncthreads();
+    if (s_abort) return;
+    float *ph = reinterpret_cast<float *>(s_wph4) + (size_t)w * 2 * kWarpSlotFloats;
+    WarpSlot *slot = s_slot[w];
+    const unsigned lt_mask = (1u << lane) - 1u;
+    int lim = 0;
+
+    // warp-uniform state: cur = the slot units are handed out from, next_u
+    // its next unit; nxt = the other slot holds a staged item not yet
+    // started; restage = the other slot is to be refilled once none of its
+    // units is in flight
+    int cur = 0, next_u = 0;
+    bool nxt = false, restage = false;
+    int it = warp_claim(a, lane);
+    if (it >= 0) {
+        warp_stage(slot[0], ph, a, it, lane);
+        cp_async_wait_all();
+        __syncwarp();
+        it = warp_claim(a, lane);
+        if (it >= 0) {
+            warp_stage(slot[1], ph + kWarpSlotFloats, a, it, lane);
+            nxt = true;
+        }
+    } else {
+        slot[0].units = 0;          // nothing for this warp
+        __syncwarp();
+    }
+
+    Unit U;
+    int us = 0;                     // the slot of the lane's unit
+    bool active = false, need = true;
+    for (;;) {
+        // lanes without a unit take the next ones, from the current item
+        // and then from the staged one
+        unsigned needm = __ballot_sync(0xffffffffu, need);
+        while (needm) {
+            const int avail = slot[cur].units - next_u;
+            if (avail <= 0) {
+                if (!nxt) break;            // nothing staged: these lanes idle
+                cp_async_wait_all();
+                __syncwarp();
+                cur ^= 1;
+                next_u = 0;
+                nxt = false;
+                restage = true;
+                continue;
+            }
+            const int rank = __popc(needm & lt_mask);
+            const bool take = need && rank < avail;
+            if (take) {
+                const WarpSlot &S = slot[cur];
+                unit_begin(U, next_u + rank, a.S, sdiv(s_Sm, s_Sl), S.tb0, S.sN, S.sT, a.seed,
+                           a.pbase + (uint32_t)S.p);
+                us = cur;
+                active = true;
+                need = false;
+            }
+            const unsigned took = __ballot_sync(0xffffffffu, take);
+            next_u += __popc(took);
+            needm &= ~took;
+        }
+        // refill the other slot once none of its units is in flight
+        if (restage && !__any_sync(0xffffffffu, active && us != cur)) {
+            restage = false;
+            it = warp_claim(a, lane);
+            if (it >= 0) {
+                warp_stage(slot[cur ^ 1], ph + (cur ^ 1) * kWarpSlotFloats, a, it, lane);
+                nxt = true;
+            }
+        }
+        if (!__any_sync(0xffffffffu, active)) {
+            // no unit in flight: the warp is done unless a staged item waits
+            if (!nxt && slot[cur].units - next_u <= 0) break;
+            continue;
+        }
+        bool fin = false;
+        int bin = -1;
+        if (active) {
+            const WarpSlot &S = slot[us];
+            fin = U.done;
+            if (!fin) {
+                const float *offs = S.staged ? (ph + us * kWarpSlotFloats + S.sOff[U.lb])
+                                             : (a.offsets + a.off_idx[S.tb0 + U.lb]);
+                const DevParams &P = s_par[S.p];
+                fin = step_pho(U, P, offs, a.gamma, a.ct, a.r0, s_bgc, lim, s_inv,
+                               a.bcdf + (size_t)S.p * P.n * kTableRows,
+                               a.bguide + (size_t)S.p * P.n * kTableRows);
+            }
+            if (fin) {
+                const int64_t b = S.tb0 + U.lb;
+                if (a.unit_out) a.unit_out[((int64_t)S.p * (a.b1 - a.b0) + (b - a.b0)) * a.S + U.s] = U.A;
+                if (U.Nb > 0 && U.A >= 0) bin = S.p * a.nbins + pr_bin(U.A, U.Nb, a.nbins);
+                active = false;
+                need = true;
+            }
+        }
+        if (bin >= 0) atomicAdd(&sh[bin], 1u);
+    }
+    cp_async_wait_all();
+    __syncthreads();
+    for (int i = tid; i < a.P * a.nbins; i += kThreads) {
+        const unsigned v = sh[i];
+        if (v) atomicAdd(a.hist + i, (unsigned long long)v);
+    }
+    if (lim) atomicAdd(a.limit_hits, (unsigned long long)lim);
+    if (a.chi2) last_cta_chi2(a);
+}
+
 __global__ void chi2_kernel(const unsigned long long *hist, const float *obs, int P, int nbins,
                             int left_pad, int S, int n_states, double *chi2) {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1082,7 +1301,18 @@ const void *pda_kernel_fn(int mode) {
                      : reinterpret_cast<const void *>(&pda_kernel<1>);
 }
 
+size_t photon_warp_smem() { return sizeof(float) * (size_t)kWarpSlotFloats * 2 * (kThreads / 32); }
+
+bool photon_warp_eligible(const PdaArgs &a) {
+    return a.w_tile > 0 && a.vflag == nullptr && a.done_target == 0u && a.P <= kWarpParSets &&
+           a.P * a.nbins <= kHistBins && a.hN == nullptr;
+}
+
 cudaError_t launch_pda(int mode, const PdaArgs &a, int grid, size_t dyn_smem, cudaStream_t st) {
+    if (mode == 1 && photon_warp_eligible(a)) {
+        pda_photon_warp_kernel<<<a.w_grid, kThreads, photon_warp_smem(), st>>>(a);
+        return cudaGetLastError();
+    }
     if (mode == 0) pda_kernel<0><<<grid, kThreads, dyn_smem, st>>>(a);
     else if (mode == kModePhotonDirect) pda_kernel<2><<<grid, kThreads, dyn_smem, st>>>(a);
     else pda_kernel<1><<<grid, kThreads, dyn_smem, st>>>(a);
@@ -1091,6 +1321,8 @@ cudaError_t launch_pda(int mode, const PdaArgs &a, int grid, size_t dyn_smem, cu
 
 cudaError_t pda_set_smem_limit(int mode, size_t dyn_smem) {
     if (mode == 0) return cudaFuncSetAttribute(pda_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn_smem);
+    if (mode == kModePhotonWarp)
+        return cudaFuncSetAttribute(pda_photon_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn_smem);
     if (mode == kModePhotonDirect)
         return cudaFuncSetAttribute(pda_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn_smem);
     return cudaFuncSetAttribute(pda_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn_smem);
@@ -1098,6 +1330,8 @@ cudaError_t pda_set_smem_limit(int mode, size_t dyn_smem) {
 
 cudaError_t pda_occupancy_blocks(int mode, size_t dyn_smem, int *blocks_per_sm) {
     if (mode == 0) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, pda_kernel<0>, kThreads, dyn_smem);
+    if (mode == kModePhotonWarp)
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, pda_photon_warp_kernel, kThreads, dyn_smem);
     if (mode == kModePhotonDirect)
         return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, pda_kernel<2>, kThreads, dyn_smem);
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, pda_kernel<1>, kThreads, dyn_smem);
