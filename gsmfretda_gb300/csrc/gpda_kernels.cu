@@ -773,7 +773,10 @@ __device__ __forceinline__ void warp_stage(WarpSlot &S, float *ph, const PdaArgs
     __syncwarp();
 }
 
-__global__ void __launch_bounds__(kThreads, kMinBlocks) pda_photon_warp_kernel(const PdaArgs a) {
+#ifndef GPDA_WARP_MIN_BLOCKS
+#define GPDA_WARP_MIN_BLOCKS 4
+#endif
+__global__ void __launch_bounds__(kThreads, GPDA_WARP_MIN_BLOCKS) pda_photon_warp_kernel(const PdaArgs a) {
     extern __shared__ float4 s_wph4[];
     constexpr int kWarps = kThreads / 32;
     __shared__ WarpSlot s_slot[kWarps][2];
