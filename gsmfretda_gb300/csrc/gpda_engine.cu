@@ -316,7 +316,7 @@ int range_args(gpda_ctx *c, int mode, int P, int n, int64_t b0, int64_t b1, int 
     // photon mode: the warp-pipelined kernel's items (about GPDA_WARP_UNITS
     // units each, 6 to 8 per lane), used unless the caller asks for in-kernel
     // store checks (launch_pda decides)
-    if (mode == GPDA_MODE_PHOTON) {
+    if (mode == GPDA_MODE_PHOTON && photon_warp_eligible(P, a.nbins)) {
         const int wt = std::max(1, std::min(kWarpTileMax, (GPDA_WARP_UNITS + S - 1) / S));
         const int64_t wn = (b1 - b0 + wt - 1) / wt;
         if (wn * P <= (int64_t)INT32_MAX) {
@@ -325,6 +325,8 @@ int range_args(gpda_ctx *c, int mode, int P, int n, int64_t b0, int64_t b1, int 
             a.w_items = (int)(wn * P);
             a.w_grid = (int)std::min<int64_t>((a.w_items + kThreads / 32 - 1) / (kThreads / 32),
                                               (int64_t)c->num_sms * c->blocks_per_sm[kModePhotonWarp]);
+            grid = a.w_grid;
+            return GPDA_OK;
         }
     }
 #endif

@@ -80,9 +80,9 @@ struct PdaArgs {
     // tiles of tile_s bursts of every parameter set (a shorter tail when the
     // last items finish); tile_s = 0: ntiles tiles of tile_b bursts
     int32_t nbig, nsmall, tile_s;
-    // photon mode, warp-pipelined kernel (w_tile > 0, used when no in-kernel
-    // store checks are asked for): items of w_tile bursts of one parameter
-    // set, w_ntiles per set, w_items in all, on a grid of w_grid CTAs
+    // photon mode, warp-pipelined kernel (w_tile > 0): items of w_tile
+    // bursts of one parameter set, w_ntiles per set, w_items in all, on a
+    // grid of w_grid CTAs
     int32_t w_tile, w_ntiles, w_items, w_grid;
     int32_t nbins;
     int32_t smem_cap;             // photon staging capacity (floats)
@@ -147,7 +147,7 @@ struct RcArgs {
 // kernel launchers (gpda_kernels.cu); launch mode kModePhotonDirect is photon
 // mode with direct reads of host arrays (PdaArgs::hN); kModePhotonWarp is the
 // warp-pipelined photon kernel (launch_pda picks it for photon mode when
-// PdaArgs::w_tile > 0 and no store checks are asked for)
+// PdaArgs::w_tile > 0 and the tile is not read from host memory)
 constexpr int kModePhotonDirect = 2;
 constexpr int kModePhotonWarp = 3;
 // warp-pipelined photon kernel: bursts per warp item at most, parameter sets
@@ -168,7 +168,7 @@ cudaError_t launch_validate(const int32_t *N, const float *T, const int64_t *off
                             int num_sms, cudaStream_t st);
 cudaError_t pda_occupancy_blocks(int mode, size_t dyn_smem, int *blocks_per_sm);
 size_t photon_warp_smem();                 // dynamic shared memory of the warp-pipelined kernel
-bool photon_warp_eligible(const PdaArgs &a);
+bool photon_warp_eligible(int P, int nbins);  // parameter sets and bins the warp kernel holds
 cudaError_t pda_set_smem_limit(int mode, size_t dyn_smem);
 
 // host parameter derivation (gpda_params.cpp)

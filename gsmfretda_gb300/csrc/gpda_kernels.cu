@@ -732,16 +732,46 @@ __device__ __forceinline__ int warp_claim(const PdaArgs &a, int lane) {
 
 // Stage work item `item` into slot S (offsets into ph, cap floats): the
 // bursts' counts, durations and offset starts now; the offsets' 16-byte
-// span with cp.async (committed, not waited for). Whole warp.
+// span with cp.async (committed, not waited for). Whole warp. kCheck: the
+// store checks of validate_kernel on the item's counts, durations and
+// offset starts first (error bits into *a.vflag); an item that fails gets
+// no units and no copy.
+template <bool kCheck>
 __device__ __forceinline__ void warp_stage(WarpSlot &S, float *ph, const PdaArgs &a, int item, int lane) {
     const int p = item / a.w_ntiles;
     const int64_t tb0 = a.b0 + (int64_t)(item - p * a.w_ntiles) * a.w_tile;
     const int nb = (int)min((int64_t)a.w_tile, a.b1 - tb0);
     int64_t oi = 0;
+    int32_t n_ = 0;
+    float t_ = 0.0f;
     if (lane <= nb) oi = a.off_idx[tb0 + lane];
     if (lane < nb) {
-        S.sN[lane] = a.N[tb0 + lane];
-        S.sT[lane] = a.T[tb0 + lane];
+        n_ = a.N[tb0 + lane];
+        t_ = a.T[tb0 + lane];
+        S.sN[lane] = n_;
+        S.sT[lane] = t_;
+    }
+    if (kCheck) {
+        const int64_t oi1 = __shfl_down_sync(0xffffffffu, oi, 1);
+        unsigned bad = 0u;
+        if (lane < nb) {
+            if (n_ < 0 || n_ > (1 << 21)) bad |= 1u;
+            if (!(t_ >= 0.0f) || !isfinite(t_)) bad |= 2u;
+            if (oi1 - oi != (int64_t)n_ || oi < 0 || oi1 > a.nph) bad |= 4u;
+        }
+        bad = __reduce_or_sync(0xffffffffu, bad);
+        if (bad) {
+            if (lane == 0) {
+                atomicOr(a.vflag, bad);
+                S.tb0 = tb0;
+                S.p = p;
+                S.nb = nb;
+                S.units = 0;
+                S.staged = 0;
+            }
+            __syncwarp();
+            return;
+        }
     }
     const int64_t first = __shfl_sync(0xffffffffu, oi, 0);
     const int64_t last = __shfl_sync(0xffffffffu, oi, nb);
@@ -776,6 +806,33 @@ __device__ __forceinline__ void warp_stage(WarpSlot &S, float *ph, const PdaArgs
 #ifndef GPDA_WARP_MIN_BLOCKS
 #define GPDA_WARP_MIN_BLOCKS 4
 #endif
+// A staged item becomes current (its copy has landed): kCheck: the offsets
+// of each burst finite and sorted (validate_kernel's bits 8, 16); an item
+// that fails gets no units. Whole warp.
+template <bool kCheck>
+__device__ __forceinline__ void warp_open(WarpSlot &S, const float *ph, const PdaArgs &a, int lane) {
+    if (!kCheck || S.units == 0) return;
+    unsigned bad = 0u;
+    for (int i = 0; i < S.nb; ++i) {
+        const float *o = S.staged ? (ph + S.sOff[i]) : (a.offsets + a.off_idx[S.tb0 + i]);
+        const int n_ = S.sN[i];
+        for (int j = lane; j < n_; j += 32) {
+            const float x = o[j];
+            if (!isfinite(x)) bad |= 8u;
+            if (j > 0 && x < o[j - 1]) bad |= 16u;
+        }
+    }
+    bad = __reduce_or_sync(0xffffffffu, bad);
+    if (bad) {
+        if (lane == 0) {
+            atomicOr(a.vflag, bad);
+            S.units = 0;
+        }
+    }
+    __syncwarp();
+}
+
+template <bool kCheck>
 __global__ void __launch_bounds__(kThreads, GPDA_WARP_MIN_BLOCKS) pda_photon_warp_kernel(const PdaArgs a) {
     extern __shared__ float4 s_wph4[];
     constexpr int kWarps = kThreads / 32;
@@ -820,12 +877,13 @@ __global__ void __launch_bounds__(kThreads, GPDA_WARP_MIN_BLOCKS) pda_photon_war
     bool nxt = false, restage = false;
     int it = warp_claim(a, lane);
     if (it >= 0) {
-        warp_stage(slot[0], ph, a, it, lane);
+        warp_stage<kCheck>(slot[0], ph, a, it, lane);
         cp_async_wait_all();
         __syncwarp();
+        warp_open<kCheck>(slot[0], ph, a, lane);
         it = warp_claim(a, lane);
         if (it >= 0) {
-            warp_stage(slot[1], ph + kWarpSlotFloats, a, it, lane);
+            warp_stage<kCheck>(slot[1], ph + kWarpSlotFloats, a, it, lane);
             nxt = true;
         }
     } else {
@@ -850,6 +908,7 @@ __global__ void __launch_bounds__(kThreads, GPDA_WARP_MIN_BLOCKS) pda_photon_war
                 next_u = 0;
                 nxt = false;
                 restage = true;
+                warp_open<kCheck>(slot[cur], ph + cur * kWarpSlotFloats, a, lane);
                 continue;
             }
             const int rank = __popc(needm & lt_mask);
@@ -871,7 +930,7 @@ __global__ void __launch_bounds__(kThreads, GPDA_WARP_MIN_BLOCKS) pda_photon_war
             restage = false;
             it = warp_claim(a, lane);
             if (it >= 0) {
-                warp_stage(slot[cur ^ 1], ph + (cur ^ 1) * kWarpSlotFloats, a, it, lane);
+                warp_stage<kCheck>(slot[cur ^ 1], ph + (cur ^ 1) * kWarpSlotFloats, a, it, lane);
                 nxt = true;
             }
         }
@@ -1306,14 +1365,12 @@ const void *pda_kernel_fn(int mode) {
 
 size_t photon_warp_smem() { return sizeof(float) * (size_t)kWarpSlotFloats * 2 * (kThreads / 32); }
 
-bool photon_warp_eligible(const PdaArgs &a) {
-    return a.w_tile > 0 && a.vflag == nullptr && a.done_target == 0u && a.P <= kWarpParSets &&
-           a.P * a.nbins <= kHistBins && a.hN == nullptr;
-}
+bool photon_warp_eligible(int P, int nbins) { return P <= kWarpParSets && P * nbins <= kHistBins; }
 
 cudaError_t launch_pda(int mode, const PdaArgs &a, int grid, size_t dyn_smem, cudaStream_t st) {
-    if (mode == 1 && photon_warp_eligible(a)) {
-        pda_photon_warp_kernel<<<a.w_grid, kThreads, photon_warp_smem(), st>>>(a);
+    if (mode == 1 && a.w_tile > 0 && a.hN == nullptr) {
+        if (a.vflag) pda_photon_warp_kernel<true><<<grid, kThreads, photon_warp_smem(), st>>>(a);
+        else pda_photon_warp_kernel<false><<<grid, kThreads, photon_warp_smem(), st>>>(a);
         return cudaGetLastError();
     }
     if (mode == 0) pda_kernel<0><<<grid, kThreads, dyn_smem, st>>>(a);
@@ -1325,7 +1382,11 @@ cudaError_t launch_pda(int mode, const PdaArgs &a, int grid, size_t dyn_smem, cu
 cudaError_t pda_set_smem_limit(int mode, size_t dyn_smem) {
     if (mode == 0) return cudaFuncSetAttribute(pda_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn_smem);
     if (mode == kModePhotonWarp)
-        return cudaFuncSetAttribute(pda_photon_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn_smem);
+    {
+        cudaError_t e = cudaFuncSetAttribute(pda_photon_warp_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn_smem);
+        if (e != cudaSuccess) return e;
+        return cudaFuncSetAttribute(pda_photon_warp_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn_smem);
+    }
     if (mode == kModePhotonDirect)
         return cudaFuncSetAttribute(pda_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn_smem);
     return cudaFuncSetAttribute(pda_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn_smem);
@@ -1334,7 +1395,7 @@ cudaError_t pda_set_smem_limit(int mode, size_t dyn_smem) {
 cudaError_t pda_occupancy_blocks(int mode, size_t dyn_smem, int *blocks_per_sm) {
     if (mode == 0) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, pda_kernel<0>, kThreads, dyn_smem);
     if (mode == kModePhotonWarp)
-        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, pda_photon_warp_kernel, kThreads, dyn_smem);
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, pda_photon_warp_kernel<true>, kThreads, dyn_smem);
     if (mode == kModePhotonDirect)
         return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, pda_kernel<2>, kThreads, dyn_smem);
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, pda_kernel<1>, kThreads, dyn_smem);
