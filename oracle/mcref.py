@@ -28,7 +28,7 @@ def load(path=None):
         vp, i32, i64, f32 = C.c_void_p, C.c_int32, C.c_int64, C.c_float
         lib.mcref_run.restype = C.c_int
         lib.mcref_run.argtypes = [vp, vp, vp, vp, i64, vp, vp, i64, vp, f32, f32, f32, i32,
-                                  vp, vp, vp, vp, vp, i32, i32, vp, vp, vp]
+                                  vp, vp, vp, vp, vp, i32, i32, vp, vp, vp, i32]
         _lib = lib
     return _lib
 
@@ -43,7 +43,7 @@ def tables(n, args, m):
             np.array(p.pinit[:n], dtype=np.float32))
 
 
-def run(d, n, args, m, R, tape_cap=0):
+def run(d, n, args, m, R, tape_cap=0, debug=False):
     """mc_kernel over all bursts of the reference-layout burst data d with R
     (a power of two) samples per burst. Returns mcE[B*R] and, with tape_cap,
     the per-thread draw tapes (orc.TAPE_DTYPE[B*R, tape_cap]) and lengths."""
@@ -61,7 +61,7 @@ def run(d, n, args, m, R, tape_cap=0):
     rc = lib.mcref_run(p(arr["start"]), p(arr["stop"]), p(arr["istart"]), p(arr["phCount"]), B,
                        p(arr["burst_ad"]), p(arr["burst_dd"]), arr["burst_ad"].size, p(arr["T"]),
                        d["clk_p"], d["bg_ad_rate"], d["bg_dd_rate"], n, p(gpe), p(gpv), p(gpk),
-                       p(gpij), p(gpp), R, tape_cap, p(mcE), p(tape), p(tlen))
+                       p(gpij), p(gpp), R, tape_cap, p(mcE), p(tape), p(tlen), 1 if debug else 0)
     if rc != 0:
         raise RuntimeError(f"mcref_run rc={rc}")
     return mcE, tape, tlen

@@ -106,13 +106,26 @@ __device__ long rec_rk_binomial(rk_state *st, int n, double p) {
     tape_put(kB | (n << 8), (int32_t)v, p);
     return v;
 }
+// diagnostics (g_tape_debug): draw_P_B_Tr's time bin and photon total as
+// the kernel passes them (kinds 7 and 8, before the call's own records)
+__device__ int32_t g_tape_debug;
+__device__ bool rec_draw_P_B_Tr(float *bc, float *totPhoton, int timebin, float *timesp, float bg_rate,
+                                curandStateScrambledSobol64 *state) {
+    if (g_tape_debug) {
+        tape_put(7, 0, (double)*timesp);
+        tape_put(8, 0, (double)*totPhoton);
+    }
+    return draw_P_B_Tr(bc, totPhoton, timebin, timesp, bg_rate, state);
+}
 #define drawTau rec_drawTau
 #define drawE rec_drawE
 #define rk_binomial rec_rk_binomial
+#define draw_P_B_Tr rec_draw_P_B_Tr
 #include "mc_kernel.inc"
 #undef drawTau
 #undef drawE
 #undef rk_binomial
+#undef draw_P_B_Tr
 
 // ---------------------------------------------------------------- host
 namespace {
@@ -132,7 +145,8 @@ extern "C" {
 // Runs setup_kernel + mc_kernel over bursts [0, nb) with R (a power of two)
 // samples per burst, as mc::init_randstate and mc::run_kernel do, and copies
 // mcE[nb * R] back. tape_cap > 0: the draws of thread t go to
-// tape[t * tape_cap ...] (16-byte records) and their count to tape_len[t].
+// tape[t * tape_cap ...] (16-byte records) and their count to tape_len[t];
+// debug != 0 adds the diagnostic records (kinds 7, 8; not replayable).
 // Returns 0, or a CUDA / cuRAND error code (message on stderr).
 int mcref_run(const int64_t *start, const int64_t *stop, const int64_t *istart,
               const int32_t *phCount, int64_t nb, const int64_t *burst_ad,
@@ -140,7 +154,7 @@ int mcref_run(const int64_t *start, const int64_t *stop, const int64_t *istart,
               float bg_ad_rate, float bg_dd_rate, int32_t s_n, const float *gpe,
               const float *gpv, const float *gpk, const float *gpp_i2j, const float *gpp,
               int32_t R, int32_t tape_cap, float *mcE_out, void *tape_out,
-              int32_t *tape_len_out) {
+              int32_t *tape_len_out, int32_t debug) {
     if (nb < 1 || R < 1 || (R & (R - 1)) != 0 || s_n < 2 || nb * (int64_t)R > (1 << 22)) return -1;
     const int NN = (int)(nb * R);
     int err = 0;
@@ -203,6 +217,7 @@ int mcref_run(const int64_t *start, const int64_t *stop, const int64_t *istart,
         cudaMemcpyToSymbol(g_tape, &d_tape, sizeof(d_tape));
         cudaMemcpyToSymbol(g_tape_len, &d_tlen, sizeof(d_tlen));
         cudaMemcpyToSymbol(g_tape_cap, &tape_cap, sizeof(tape_cap));
+        cudaMemcpyToSymbol(g_tape_debug, &debug, sizeof(debug));
         mc_kernel<<<grid, blockSize>>>(d_start, d_stop, d_ad, d_dd, d_istart, d_ph, d_T, clk_p,
                                        bg_ad_rate, bg_dd_rate, d_e, d_v, d_k, d_pij, d_p, d_scratch,
                                        (int)nb, s_n, d_q, d_states, d_mcE, R);
