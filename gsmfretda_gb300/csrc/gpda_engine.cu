@@ -100,7 +100,7 @@ struct gpda_ctx {
     int last_P = 0;
     bool last_chi2 = false;
     int64_t launches = 0;
-    int blocks_per_sm[4] = {0, 0, 0, 0};   // resident CTAs per SM by launch mode
+    int blocks_per_sm[3] = {0, 0, 0};   // resident CTAs per SM by launch mode
     std::string err;
 };
 
@@ -185,21 +185,10 @@ int ensure_scratch(gpda_ctx *c, int P) {
 // set otherwise leaves CTAs idle at the end), down to one round of kThreads
 // units. Photon mode keeps its tiles: there a lane takes the tile's next unit
 // as soon as its own is done, and tiles of fewer units per lane measured
-// slower than the end-of-launch imbalance they remove.
+// slower than the end-of-launch imbalance they remove. GPDA_TILE_UNITS (a
+// build option) sets the ~2048.
 #ifndef GPDA_TILE_UNITS
 #define GPDA_TILE_UNITS 2048
-#endif
-#ifndef GPDA_TAIL_DIV
-#define GPDA_TAIL_DIV 0
-#endif
-#ifndef GPDA_PHOTON_WARP
-#define GPDA_PHOTON_WARP 0
-#endif
-#ifndef GPDA_WARP_UNITS
-#define GPDA_WARP_UNITS 200
-#endif
-#ifndef GPDA_TAIL_WAVES
-#define GPDA_TAIL_WAVES 1
 #endif
 
 int tile_bursts(const gpda_ctx *c, int mode, int S, int64_t nb, int P) {
@@ -312,44 +301,6 @@ int range_args(gpda_ctx *c, int mode, int P, int n, int64_t b0, int64_t b1, int 
     }
     a.abort_flag = abort_flag;
     grid = (int)std::min<int64_t>(a.n_items, (int64_t)c->num_sms * c->blocks_per_sm[mode]);
-#if GPDA_PHOTON_WARP
-    // photon mode: the warp-pipelined kernel's items (about GPDA_WARP_UNITS
-    // units each, 6 to 8 per lane), used unless the caller asks for in-kernel
-    // store checks (launch_pda decides)
-    if (mode == GPDA_MODE_PHOTON && photon_warp_eligible(P, a.nbins)) {
-        const int wt = std::max(1, std::min(kWarpTileMax, (GPDA_WARP_UNITS + S - 1) / S));
-        const int64_t wn = (b1 - b0 + wt - 1) / wt;
-        if (wn * P <= (int64_t)INT32_MAX) {
-            a.w_tile = wt;
-            a.w_ntiles = (int)wn;
-            a.w_items = (int)(wn * P);
-            a.w_grid = (int)std::min<int64_t>((a.w_items + kThreads / 32 - 1) / (kThreads / 32),
-                                              (int64_t)c->num_sms * c->blocks_per_sm[kModePhotonWarp]);
-            grid = a.w_grid;
-            return GPDA_OK;
-        }
-    }
-#endif
-#if GPDA_TAIL_DIV > 0
-    // photon mode: the last ~GPDA_TAIL_WAVES items' worth of bursts per CTA
-    // in tiles GPDA_TAIL_DIV times smaller, handed out last
-    if (mode == GPDA_MODE_PHOTON && a.tile_b >= 2 * GPDA_TAIL_DIV) {
-        const int64_t nb_all = b1 - b0;
-        const int ts = a.tile_b / GPDA_TAIL_DIV;
-        const int64_t tail = ((int64_t)grid * a.tile_b * GPDA_TAIL_WAVES + P - 1) / P;
-        if (tail < nb_all) {
-            const int64_t nbig = (nb_all - tail) / a.tile_b;
-            const int64_t nsmall = (nb_all - nbig * a.tile_b + ts - 1) / ts;
-            if ((nbig + nsmall) * P <= (int64_t)INT32_MAX && nbig > 0) {
-                a.tile_s = ts;
-                a.nbig = (int)nbig;
-                a.nsmall = (int)nsmall;
-                a.n_items = (int)((nbig + nsmall) * P);
-                grid = (int)std::min<int64_t>(a.n_items, (int64_t)c->num_sms * c->blocks_per_sm[mode]);
-            }
-        }
-    }
-#endif
     return GPDA_OK;
 }
 
@@ -669,10 +620,7 @@ gpda_ctx *gpda_create(int32_t device, const gpda_model *m, int32_t *status) {
     if (bad(pda_occupancy_blocks(1, sizeof(float) * kSmemCapFloats, &c->blocks_per_sm[1]))) return nullptr;
     if (bad(pda_occupancy_blocks(kModePhotonDirect, sizeof(float) * kSmemCapFloats,
                                  &c->blocks_per_sm[kModePhotonDirect]))) return nullptr;
-    if (bad(pda_set_smem_limit(kModePhotonWarp, photon_warp_smem()))) return nullptr;
-    if (bad(pda_occupancy_blocks(kModePhotonWarp, photon_warp_smem(), &c->blocks_per_sm[kModePhotonWarp])))
-        return nullptr;
-    for (int i = 0; i < 4; ++i) c->blocks_per_sm[i] = std::max(1, c->blocks_per_sm[i]);
+    for (int i = 0; i < 3; ++i) c->blocks_per_sm[i] = std::max(1, c->blocks_per_sm[i]);
     set(GPDA_OK);
     return c;
 }

@@ -74,16 +74,7 @@ struct PdaArgs {
     int32_t S;
     int32_t tile_b;               // bursts per work item
     int32_t ntiles;
-    int32_t n_items;              // ntiles * P, or P * (nbig + nsmall)
-    // tile_s > 0: the range ends in smaller work items, handed out last: the
-    // first nbig tiles of tile_b bursts of every parameter set, then nsmall
-    // tiles of tile_s bursts of every parameter set (a shorter tail when the
-    // last items finish); tile_s = 0: ntiles tiles of tile_b bursts
-    int32_t nbig, nsmall, tile_s;
-    // photon mode, warp-pipelined kernel (w_tile > 0): items of w_tile
-    // bursts of one parameter set, w_ntiles per set, w_items in all, on a
-    // grid of w_grid CTAs
-    int32_t w_tile, w_ntiles, w_items, w_grid;
+    int32_t n_items;              // ntiles * P
     int32_t nbins;
     int32_t smem_cap;             // photon staging capacity (floats)
     uint32_t pbase;               // parameter-set word of the counter = pbase + p
@@ -145,17 +136,8 @@ struct RcArgs {
 };
 
 // kernel launchers (gpda_kernels.cu); launch mode kModePhotonDirect is photon
-// mode with direct reads of host arrays (PdaArgs::hN); kModePhotonWarp is the
-// warp-pipelined photon kernel (launch_pda picks it for photon mode when
-// PdaArgs::w_tile > 0 and the tile is not read from host memory)
+// mode with direct reads of host arrays (PdaArgs::hN)
 constexpr int kModePhotonDirect = 2;
-constexpr int kModePhotonWarp = 3;
-// warp-pipelined photon kernel: bursts per warp item at most, parameter sets
-// it holds in shared memory, and shared-memory staging per slot (floats);
-// each of the 8 warps keeps two slots
-constexpr int kWarpTileMax = 8;
-constexpr int kWarpParSets = 4;
-constexpr int kWarpSlotFloats = 704;
 cudaError_t launch_pda(int mode, const PdaArgs &a, int grid, size_t dyn_smem, cudaStream_t st);
 const void *pda_kernel_fn(int mode);   // the kernel launch_pda(mode) runs
 cudaError_t launch_chi2(const unsigned long long *hist, const float *obs, int P, int nbins,
@@ -167,8 +149,6 @@ cudaError_t launch_validate(const int32_t *N, const float *T, const int64_t *off
                             const float *offsets, int64_t B, int64_t nph, unsigned int *flag,
                             int num_sms, cudaStream_t st);
 cudaError_t pda_occupancy_blocks(int mode, size_t dyn_smem, int *blocks_per_sm);
-size_t photon_warp_smem();                 // dynamic shared memory of the warp-pipelined kernel
-bool photon_warp_eligible(int P, int nbins);  // parameter sets and bins the warp kernel holds
 cudaError_t pda_set_smem_limit(int mode, size_t dyn_smem);
 
 // host parameter derivation (gpda_params.cpp)

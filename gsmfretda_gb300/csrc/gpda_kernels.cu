@@ -370,20 +370,10 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) pda_kernel(const PdaArgs
         __syncthreads();
         const int item = s_item;
         if (item >= a.n_items) break;
-        int p;
-        int64_t tb0;
-        int nb;
-        if (a.tile_s == 0 || item < a.P * a.nbig) {
-            const int per = a.tile_s ? a.nbig : a.ntiles;
-            p = item / per;
-            tb0 = a.b0 + (int64_t)(item - p * per) * a.tile_b;
-            nb = (int)min((int64_t)a.tile_b, a.b1 - tb0);
-        } else {
-            const int j = item - a.P * a.nbig;
-            p = j / a.nsmall;
-            tb0 = a.b0 + (int64_t)a.nbig * a.tile_b + (int64_t)(j - p * a.nsmall) * a.tile_s;
-            nb = (int)min((int64_t)a.tile_s, a.b1 - tb0);
-        }
+        const int p = item / a.ntiles;
+        const int tile = item - p * a.ntiles;
+        const int64_t tb0 = a.b0 + (int64_t)tile * a.tile_b;
+        const int nb = (int)min((int64_t)a.tile_b, a.b1 - tb0);
         {
             const uint32_t *src = reinterpret_cast<const uint32_t *>(a.params + p);
             uint32_t *dst = reinterpret_cast<uint32_t *>(&sp);
@@ -686,287 +676,6 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) pda_kernel(const PdaArgs
             unsigned v = sh[i];
             if (v) atomicAdd(a.hist + (size_t)p * a.nbins + i, (unsigned long long)v);
         }
-    }
-    if (lim) atomicAdd(a.limit_hits, (unsigned long long)lim);
-    if (a.chi2) last_cta_chi2(a);
-}
-
-// ---------------------------------------------------------------- photon mode, warp pipelines
-// pda_photon_warp_kernel: the photon-mode simulation without the end-of-item
-// idling of pda_kernel<1>. There all 256 threads share one staged tile, and a
-// lane whose units are done waits for the slowest unit of the tile before the
-// CTA stages the next one (about a fifth of the lane-steps at 21-burst tiles).
-// Here every warp pulls its own work items (w_tile bursts of one parameter
-// set) and keeps two in shared memory: while its lanes take units from one,
-// the other is refilled as soon as its last unit is done, its arrival offsets
-// copied with cp.async, so a lane whose unit ends takes the next unit at once,
-// from whichever item has one. Everything a warp shares lives in its own two
-// slots and is decided by warp votes: no CTA barrier in the simulation loop.
-// Units, counters and results are those of pda_kernel<1> (a unit's draws
-// depend only on its (parameter set, burst, sample)). Parameter sets live in
-// shared memory (P <= kWarpParSets), the histogram too (P nbins <= kHistBins).
-struct WarpSlot {
-    int64_t tb0;
-    int32_t p, nb, units, staged;
-    int32_t sN[kWarpTileMax];
-    float sT[kWarpTileMax];
-    int32_t sOff[kWarpTileMax + 1];
-};
-
-__device__ __forceinline__ void cp_async16(void *smem, const void *gmem, int src_bytes) {
-    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(sa), "l"(gmem), "r"(src_bytes)
-                 : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
-
-// The next work item of the launch for this warp (lane 0 claims, all lanes
-// get it); -1 when none is left.
-__device__ __forceinline__ int warp_claim(const PdaArgs &a, int lane) {
-    int it = 0;
-    if (lane == 0) it = (int)atomicAdd(a.work, 1u);
-    it = __shfl_sync(0xffffffffu, it, 0);
-    return it < a.w_items ? it : -1;
-}
-
-// Stage work item `item` into slot S (offsets into ph, cap floats): the
-// bursts' counts, durations and offset starts now; the offsets' 16-byte
-// span with cp.async (committed, not waited for). Whole warp. kCheck: the
-// store checks of validate_kernel on the item's counts, durations and
-// offset starts first (error bits into *a.vflag); an item that fails gets
-// no units and no copy.
-template <bool kCheck>
-__device__ __forceinline__ void warp_stage(WarpSlot &S, float *ph, const PdaArgs &a, int item, int lane) {
-    const int p = item / a.w_ntiles;
-    const int64_t tb0 = a.b0 + (int64_t)(item - p * a.w_ntiles) * a.w_tile;
-    const int nb = (int)min((int64_t)a.w_tile, a.b1 - tb0);
-    int64_t oi = 0;
-    int32_t n_ = 0;
-    float t_ = 0.0f;
-    if (lane <= nb) oi = a.off_idx[tb0 + lane];
-    if (lane < nb) {
-        n_ = a.N[tb0 + lane];
-        t_ = a.T[tb0 + lane];
-        S.sN[lane] = n_;
-        S.sT[lane] = t_;
-    }
-    if (kCheck) {
-        const int64_t oi1 = __shfl_down_sync(0xffffffffu, oi, 1);
-        unsigned bad = 0u;
-        if (lane < nb) {
-            if (n_ < 0 || n_ > (1 << 21)) bad |= 1u;
-            if (!(t_ >= 0.0f) || !isfinite(t_)) bad |= 2u;
-            if (oi1 - oi != (int64_t)n_ || oi < 0 || oi1 > a.nph) bad |= 4u;
-        }
-        bad = __reduce_or_sync(0xffffffffu, bad);
-        if (bad) {
-            if (lane == 0) {
-                atomicOr(a.vflag, bad);
-                S.tb0 = tb0;
-                S.p = p;
-                S.nb = nb;
-                S.units = 0;
-                S.staged = 0;
-            }
-            __syncwarp();
-            return;
-        }
-    }
-    const int64_t first = __shfl_sync(0xffffffffu, oi, 0);
-    const int64_t last = __shfl_sync(0xffffffffu, oi, nb);
-    const int64_t abase = first & ~(int64_t)3;
-    const int64_t aend = (last + 3) & ~(int64_t)3;
-    const bool staged = (aend - abase) <= (int64_t)kWarpSlotFloats;
-    if (staged) {
-        if (lane <= nb) S.sOff[lane] = (int32_t)(oi - abase);
-        const int nv = (int)((aend - abase) >> 2);
-        // a caller's exactly sized array (exact_offsets) ends at a photon of
-        // some tile: the vector holding the tile's last photon is copied in
-        // part and zero-filled (no burst of this tile reads past it)
-        const int64_t vend = a.exact_offsets ? last : INT64_MAX;
-        for (int i = lane; i < nv; i += 32) {
-            const int64_t e = abase + 4 * (int64_t)i;
-            const int64_t rem = vend - e;
-            const int bytes = rem >= 4 ? 16 : (rem > 0 ? (int)rem * 4 : 0);
-            cp_async16(ph + 4 * i, a.offsets + (bytes > 0 ? e : abase), bytes);
-        }
-    }
-    cp_async_commit();
-    if (lane == 0) {
-        S.tb0 = tb0;
-        S.p = p;
-        S.nb = nb;
-        S.units = nb * a.S;
-        S.staged = staged ? 1 : 0;
-    }
-    __syncwarp();
-}
-
-#ifndef GPDA_WARP_MIN_BLOCKS
-#define GPDA_WARP_MIN_BLOCKS 4
-#endif
-// A staged item becomes current (its copy has landed): kCheck: the offsets
-// of each burst finite and sorted (validate_kernel's bits 8, 16); an item
-// that fails gets no units. Whole warp.
-template <bool kCheck>
-__device__ __forceinline__ void warp_open(WarpSlot &S, const float *ph, const PdaArgs &a, int lane) {
-    if (!kCheck || S.units == 0) return;
-    unsigned bad = 0u;
-    for (int i = 0; i < S.nb; ++i) {
-        const float *o = S.staged ? (ph + S.sOff[i]) : (a.offsets + a.off_idx[S.tb0 + i]);
-        const int n_ = S.sN[i];
-        for (int j = lane; j < n_; j += 32) {
-            const float x = o[j];
-            if (!isfinite(x)) bad |= 8u;
-            if (j > 0 && x < o[j - 1]) bad |= 16u;
-        }
-    }
-    bad = __reduce_or_sync(0xffffffffu, bad);
-    if (bad) {
-        if (lane == 0) {
-            atomicOr(a.vflag, bad);
-            S.units = 0;
-        }
-    }
-    __syncwarp();
-}
-
-template <bool kCheck>
-__global__ void __launch_bounds__(kThreads, GPDA_WARP_MIN_BLOCKS) pda_photon_warp_kernel(const PdaArgs a) {
-    extern __shared__ float4 s_wph4[];
-    constexpr int kWarps = kThreads / 32;
-    __shared__ WarpSlot s_slot[kWarps][2];
-    __shared__ DevParams s_par[kWarpParSets];
-    __shared__ unsigned int sh[kHistBins];           // [p][bin]
-    __shared__ float s_inv[kInvTable];
-    __shared__ float s_bgc[4];
-    __shared__ uint32_t s_Sm, s_Sl;
-    __shared__ int s_abort;
-    const int tid = threadIdx.x;
-    const int lane = tid & 31;
-    const int w = tid >> 5;
-    if (tid == 0) {
-        s_abort = (a.abort_flag && __ldcg(a.abort_flag) != 0u) ? 1 : 0;
-        const Divisor dS = divisor_of((uint32_t)a.S);
-        s_Sm = dS.m;
-        s_Sl = dS.l;
-        const float bgs = a.bg_a + a.bg_d;
-        const float pa = a.bg_a / bgs;
-        s_bgc[0] = bgs;
-        s_bgc[1] = pa;
-        s_bgc[2] = 1.0f / pa;
-        s_bgc[3] = 1.0f / (1.0f - pa);
-    }
-    if (tid < kInvTable) s_inv[tid] = tid > 0 ? 1.0f / (float)tid : 0.0f;
-    for (int i = tid; i < a.P * kParamWords; i += kThreads)
-        reinterpret_cast<uint32_t *>(s_par)[i] = reinterpret_cast<const uint32_t *>(a.params)[i];
-    for (int i = tid; i < a.P * a.nbins; i += kThreads) sh[i] = 0u;
-    __syncthreads();
-    if (s_abort) return;
-    float *ph = reinterpret_cast<float *>(s_wph4) + (size_t)w * 2 * kWarpSlotFloats;
-    WarpSlot *slot = s_slot[w];
-    const unsigned lt_mask = (1u << lane) - 1u;
-    int lim = 0;
-
-    // warp-uniform state: cur = the slot units are handed out from, next_u
-    // its next unit; nxt = the other slot holds a staged item not yet
-    // started; restage = the other slot is to be refilled once none of its
-    // units is in flight
-    int cur = 0, next_u = 0;
-    bool nxt = false, restage = false;
-    int it = warp_claim(a, lane);
-    if (it >= 0) {
-        warp_stage<kCheck>(slot[0], ph, a, it, lane);
-        cp_async_wait_all();
-        __syncwarp();
-        warp_open<kCheck>(slot[0], ph, a, lane);
-        it = warp_claim(a, lane);
-        if (it >= 0) {
-            warp_stage<kCheck>(slot[1], ph + kWarpSlotFloats, a, it, lane);
-            nxt = true;
-        }
-    } else {
-        slot[0].units = 0;          // nothing for this warp
-        __syncwarp();
-    }
-
-    Unit U;
-    int us = 0;                     // the slot of the lane's unit
-    bool active = false, need = true;
-    for (;;) {
-        // lanes without a unit take the next ones, from the current item
-        // and then from the staged one
-        unsigned needm = __ballot_sync(0xffffffffu, need);
-        while (needm) {
-            const int avail = slot[cur].units - next_u;
-            if (avail <= 0) {
-                if (!nxt) break;            // nothing staged: these lanes idle
-                cp_async_wait_all();
-                __syncwarp();
-                cur ^= 1;
-                next_u = 0;
-                nxt = false;
-                restage = true;
-                warp_open<kCheck>(slot[cur], ph + cur * kWarpSlotFloats, a, lane);
-                continue;
-            }
-            const int rank = __popc(needm & lt_mask);
-            const bool take = need && rank < avail;
-            if (take) {
-                const WarpSlot &S = slot[cur];
-                unit_begin(U, next_u + rank, a.S, sdiv(s_Sm, s_Sl), S.tb0, S.sN, S.sT, a.seed,
-                           a.pbase + (uint32_t)S.p);
-                us = cur;
-                active = true;
-                need = false;
-            }
-            const unsigned took = __ballot_sync(0xffffffffu, take);
-            next_u += __popc(took);
-            needm &= ~took;
-        }
-        // refill the other slot once none of its units is in flight
-        if (restage && !__any_sync(0xffffffffu, active && us != cur)) {
-            restage = false;
-            it = warp_claim(a, lane);
-            if (it >= 0) {
-                warp_stage<kCheck>(slot[cur ^ 1], ph + (cur ^ 1) * kWarpSlotFloats, a, it, lane);
-                nxt = true;
-            }
-        }
-        if (!__any_sync(0xffffffffu, active)) {
-            // no unit in flight: the warp is done unless a staged item waits
-            if (!nxt && slot[cur].units - next_u <= 0) break;
-            continue;
-        }
-        bool fin = false;
-        int bin = -1;
-        if (active) {
-            const WarpSlot &S = slot[us];
-            fin = U.done;
-            if (!fin) {
-                const float *offs = S.staged ? (ph + us * kWarpSlotFloats + S.sOff[U.lb])
-                                             : (a.offsets + a.off_idx[S.tb0 + U.lb]);
-                const DevParams &P = s_par[S.p];
-                fin = step_pho(U, P, offs, a.gamma, a.ct, a.r0, s_bgc, lim, s_inv,
-                               a.bcdf + (size_t)S.p * P.n * kTableRows,
-                               a.bguide + (size_t)S.p * P.n * kTableRows);
-            }
-            if (fin) {
-                const int64_t b = S.tb0 + U.lb;
-                if (a.unit_out) a.unit_out[((int64_t)S.p * (a.b1 - a.b0) + (b - a.b0)) * a.S + U.s] = U.A;
-                if (U.Nb > 0 && U.A >= 0) bin = S.p * a.nbins + pr_bin(U.A, U.Nb, a.nbins);
-                active = false;
-                need = true;
-            }
-        }
-        if (bin >= 0) atomicAdd(&sh[bin], 1u);
-    }
-    cp_async_wait_all();
-    __syncthreads();
-    for (int i = tid; i < a.P * a.nbins; i += kThreads) {
-        const unsigned v = sh[i];
-        if (v) atomicAdd(a.hist + i, (unsigned long long)v);
     }
     if (lim) atomicAdd(a.limit_hits, (unsigned long long)lim);
     if (a.chi2) last_cta_chi2(a);
@@ -1363,16 +1072,7 @@ const void *pda_kernel_fn(int mode) {
                      : reinterpret_cast<const void *>(&pda_kernel<1>);
 }
 
-size_t photon_warp_smem() { return sizeof(float) * (size_t)kWarpSlotFloats * 2 * (kThreads / 32); }
-
-bool photon_warp_eligible(int P, int nbins) { return P <= kWarpParSets && P * nbins <= kHistBins; }
-
 cudaError_t launch_pda(int mode, const PdaArgs &a, int grid, size_t dyn_smem, cudaStream_t st) {
-    if (mode == 1 && a.w_tile > 0 && a.hN == nullptr) {
-        if (a.vflag) pda_photon_warp_kernel<true><<<grid, kThreads, photon_warp_smem(), st>>>(a);
-        else pda_photon_warp_kernel<false><<<grid, kThreads, photon_warp_smem(), st>>>(a);
-        return cudaGetLastError();
-    }
     if (mode == 0) pda_kernel<0><<<grid, kThreads, dyn_smem, st>>>(a);
     else if (mode == kModePhotonDirect) pda_kernel<2><<<grid, kThreads, dyn_smem, st>>>(a);
     else pda_kernel<1><<<grid, kThreads, dyn_smem, st>>>(a);
@@ -1381,12 +1081,6 @@ cudaError_t launch_pda(int mode, const PdaArgs &a, int grid, size_t dyn_smem, cu
 
 cudaError_t pda_set_smem_limit(int mode, size_t dyn_smem) {
     if (mode == 0) return cudaFuncSetAttribute(pda_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn_smem);
-    if (mode == kModePhotonWarp)
-    {
-        cudaError_t e = cudaFuncSetAttribute(pda_photon_warp_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn_smem);
-        if (e != cudaSuccess) return e;
-        return cudaFuncSetAttribute(pda_photon_warp_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn_smem);
-    }
     if (mode == kModePhotonDirect)
         return cudaFuncSetAttribute(pda_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn_smem);
     return cudaFuncSetAttribute(pda_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn_smem);
@@ -1394,8 +1088,6 @@ cudaError_t pda_set_smem_limit(int mode, size_t dyn_smem) {
 
 cudaError_t pda_occupancy_blocks(int mode, size_t dyn_smem, int *blocks_per_sm) {
     if (mode == 0) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, pda_kernel<0>, kThreads, dyn_smem);
-    if (mode == kModePhotonWarp)
-        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, pda_photon_warp_kernel<true>, kThreads, dyn_smem);
     if (mode == kModePhotonDirect)
         return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, pda_kernel<2>, kThreads, dyn_smem);
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, pda_kernel<1>, kThreads, dyn_smem);

@@ -127,6 +127,10 @@ __device__ bool rec_draw_P_B_Tr(float *bc, float *totPhoton, int timebin, float 
 #undef rk_binomial
 #undef draw_P_B_Tr
 
+// The thread-to-burst shift mc_kernel computes, idx = tidx >> (int)log2((double)R)
+// (src/mc.cu:101): the same expression on the device, for R.
+__global__ void shift_probe(int R, int *out) { *out = (int)log2((double)R); }
+
 // ---------------------------------------------------------------- host
 namespace {
 
@@ -142,9 +146,26 @@ T *dev_copy(const T *h, size_t n, int *err) {
 
 extern "C" {
 
-// Runs setup_kernel + mc_kernel over bursts [0, nb) with R (a power of two)
-// samples per burst, as mc::init_randstate and mc::run_kernel do, and copies
-// mcE[nb * R] back. tape_cap > 0: the draws of thread t go to
+// The shift mc_kernel uses on this device for reSampleTimes = R (-1 on a
+// CUDA error). With this toolchain it can be one short of log2(R): then the
+// kernel gives every burst 2^shift samples and its N * R threads reach
+// bursts up to N * R / 2^shift - 1, past N.
+int mcref_shift(int32_t R) {
+    int *d = nullptr, h = -1;
+    if (cudaMalloc(&d, sizeof(int)) != cudaSuccess) return -1;
+    shift_probe<<<1, 1>>>(R, d);
+    if (cudaMemcpy(&h, d, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) h = -1;
+    cudaFree(d);
+    return h;
+}
+
+// Runs setup_kernel + mc_kernel with reSampleTimes = R (a power of two) as
+// mc::init_randstate and mc::run_kernel do, over the nb bursts given, and
+// copies the values back. The kernel's thread-to-burst shift s (mcref_shift)
+// decides the layout: it is launched for N = nb * 2^s / R bursts, so that its
+// N * R threads map onto exactly the nb bursts given, 2^s samples each, and
+// no thread reads past them; *r_eff = 2^s and mcE[nb * 2^s] is (burst,
+// sample)-major. tape_cap > 0: the draws of thread t go to
 // tape[t * tape_cap ...] (16-byte records) and their count to tape_len[t];
 // debug != 0 adds the diagnostic records (kinds 7, 8; not replayable).
 // Returns 0, or a CUDA / cuRAND error code (message on stderr).
@@ -154,9 +175,15 @@ int mcref_run(const int64_t *start, const int64_t *stop, const int64_t *istart,
               float bg_ad_rate, float bg_dd_rate, int32_t s_n, const float *gpe,
               const float *gpv, const float *gpk, const float *gpp_i2j, const float *gpp,
               int32_t R, int32_t tape_cap, float *mcE_out, void *tape_out,
-              int32_t *tape_len_out, int32_t debug) {
-    if (nb < 1 || R < 1 || (R & (R - 1)) != 0 || s_n < 2 || nb * (int64_t)R > (1 << 22)) return -1;
-    const int NN = (int)(nb * R);
+              int32_t *tape_len_out, int32_t debug, int32_t *r_eff) {
+    if (nb < 1 || R < 1 || (R & (R - 1)) != 0 || s_n < 2) return -1;
+    const int sh = mcref_shift(R);
+    if (sh < 0 || sh > 20) return -1;
+    const int64_t reff = (int64_t)1 << sh;
+    if ((nb * reff) % R != 0 || nb * reff > (1 << 22)) return -1;
+    const int nkern = (int)(nb * reff / R);          // the kernel's N
+    const int NN = (int)(nb * reff);                 // = nkern * R threads
+    *r_eff = (int32_t)reff;
     int err = 0;
     int64_t *d_start = dev_copy(start, nb, &err), *d_stop = dev_copy(stop, nb, &err);
     int64_t *d_istart = dev_copy(istart, nb, &err);
@@ -220,7 +247,7 @@ int mcref_run(const int64_t *start, const int64_t *stop, const int64_t *istart,
         cudaMemcpyToSymbol(g_tape_debug, &debug, sizeof(debug));
         mc_kernel<<<grid, blockSize>>>(d_start, d_stop, d_ad, d_dd, d_istart, d_ph, d_T, clk_p,
                                        bg_ad_rate, bg_dd_rate, d_e, d_v, d_k, d_pij, d_p, d_scratch,
-                                       (int)nb, s_n, d_q, d_states, d_mcE, R);
+                                       nkern, s_n, d_q, d_states, d_mcE, R);
         if (cudaDeviceSynchronize() != cudaSuccess) rc = 7;
     }
     if (!rc && cudaMemcpy(mcE_out, d_mcE, sizeof(float) * NN, cudaMemcpyDeviceToHost) != cudaSuccess) rc = 8;

@@ -19,6 +19,14 @@ src/gen_rand.cuh:7-25 and src/mc.cu:366-454).
    test on the per-(burst, sample) values and a chi-square homogeneity test
    on their histograms.
 
+mc_kernel maps thread tidx to burst tidx >> (int)log2((double)R)
+(src/mc.cu:101). Built here (CUDA 13, sm_103a) that shift can come out one
+short of log2(R), and then the kernel gives each burst 2^shift samples and
+its N * R threads reach bursts past N. The harness probes the shift on the
+device and launches the kernel for the number of bursts that keeps every
+thread on the bursts it was given; the comparisons use its 2^shift samples
+per burst.
+
 Skipped where the harness sources were not extracted (the reference tree is
 not mounted where oracle/build_mcref.py ran).
 """
@@ -65,15 +73,24 @@ def _case(name):
 CASES = ["2state", "3state", "3state-broadening", "no-background", "slow", "fast"]
 
 
+def test_thread_to_burst_shift(mcref):
+    """The shift the reference kernel computes on this device, reported for
+    R = 1 .. 1024; it is log2(R) or one short of it."""
+    got = {1 << k: mcref.shift(1 << k) for k in range(11)}
+    print("shift (int)log2((double)R) on this device:", got)
+    for k in range(11):
+        assert got[1 << k] in (k, k - 1), got
+
+
 @pytest.mark.parametrize("name", CASES)
 def test_oracle_replays_the_reference_kernel_bit_exact(orc, mcref, name):
     d, n, args = _case(name)
     m = orc.model()
     R = 8
     cap = 2048 if name == "fast" else 256
-    ref, tape, tlen = mcref.run(d, n, args, m, R, tape_cap=cap)
+    ref, tape, tlen, reff = mcref.run(d, n, args, m, R, tape_cap=cap)
     assert tlen.max() <= cap, tlen.max()
-    out, status, st = orc.rc_replay(d, n, args, m, R, tape, tlen, ref)
+    out, status, st = orc.rc_replay(d, n, args, m, reff, tape, tlen, ref)
     bad = np.nonzero(status)[0]
     assert st["exact"] == st["units"], (st, bad[:10], out[bad[:5]], ref[bad[:5]])
     assert st["lambda_mismatch"] == 0 and st["binom_arg_mismatch"] == 0, st
@@ -96,9 +113,9 @@ def test_dropin_matches_the_reference_in_distribution(orc, mcref, gpda_lib, name
     d = synth.photon_stream(B=16384, seed=23)
     m = orc.model()
     R = 16
-    ref, _, _ = mcref.run(d, n, args, m, R)
+    ref, _, _, reff = mcref.run(d, n, args, m, R)
     pdamc = mc(0, 2)
-    pdamc.set_reSampleTimes(R)
+    pdamc.set_reSampleTimes(reff)
     pdamc.set_seed(777)
     pdamc.init_data_gpu(d["istart"], d["start"], d["stop"], d["phCount"], d["times"].size,
                         d["burst_ad"], d["burst_dd"], d["T"], synth.sgdivsr(d), d["clk_p"],
