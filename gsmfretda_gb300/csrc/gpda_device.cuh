@@ -366,6 +366,11 @@ __device__ __forceinline__ int binom_pre(Rng &r, int n, float p, float pp, float
     return flip ? n - x : x;
 }
 
+#ifndef GPDA_PINV_UNROLL
+#define GPDA_PINV_UNROLL 10
+#endif
+static_assert(GPDA_PINV_UNROLL >= 1 && GPDA_PINV_UNROLL <= 10, "the inversion's unrolled head");
+
 // Poisson by sequential-search inversion, lam < 10. RES: also the residual
 // of the accepted uniform inside the drawn count's interval,
 // res = (u - F(k-1)) / P(k), uniform on (0, 1] given k.
@@ -378,11 +383,12 @@ __device__ __forceinline__ int pinv_t(Rng &r, float lam, int &lim, const float *
         int k = 0;
         float f = L;
         float u = r.u01();
-        // k = 1..10 unrolled with immediate reciprocals (the same values as
-        // inv[k]); the bound is >= 10, so it is first tested at k = 11
+        // k = 1..GPDA_PINV_UNROLL (<= 10) unrolled with immediate
+        // reciprocals (the same values as inv[k]); the bound is >= 10, so it
+        // cannot stop the search before k = 11
         bool more = u > f;
 #pragma unroll
-        for (int j = 1; j <= 10; ++j) {
+        for (int j = 1; j <= GPDA_PINV_UNROLL; ++j) {
             if (more) {
                 u = u - f;
                 k = j;
