@@ -49,16 +49,17 @@ WORKLOAD = "photon_3state"
 B_FULL = 100_000
 SAMPLES = 100
 HELD_OUT_SEED = 0x0B5E
-# Algorithmic operations per unit: the fixed cost model of
+# Algorithmic operations per unit come from the fixed cost model of
 # gsmfretda_gb300/roofline.py evaluated on the workload (its mean segments per
 # unit from the stationary jump flux of the parameter set, its mean photons).
-# Thread instructions the kernel issues per unit, from ncu (captured before the
-# segment's Philox block was generated inline; warp instructions x
-# active threads per instruction / units; profiles/pda_kernel_photon_3state.txt).
-ISSUED_INST_PER_UNIT = 1000.0
-# DRAM bytes (read + write) of one MC launch on this workload, from the same
-# ncu capture; the algorithmic figure is computed live below.
-NCU_TRAFFIC_BYTES = 68.36e6
+# Thread instructions the kernel executes per unit, from one ncu capture of a
+# full launch of pda_kernel<1> on this workload (524.7 M warp instructions x
+# 18.66 active threads per instruction / 1e7 units;
+# profiles/pda_kernel_photon_3state.txt).
+ISSUED_INST_PER_UNIT = 979.1
+# DRAM bytes (read + write) of that launch (67.84 MB + 0.83 MB); the
+# algorithmic figure is computed live below.
+NCU_TRAFFIC_BYTES = 68.67e6
 
 
 def parse():
