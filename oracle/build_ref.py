@@ -10,7 +10,8 @@ import os
 import subprocess
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_SRC = os.environ.get("GPDA_REFERENCE_SRC", "/root/reference/src")
+# the reference tree's mount point (GPDA_REFERENCE overrides it), as in build_mcref.py
+REF_SRC = os.path.join(os.environ.get("GPDA_REFERENCE", "/root/reference"), "src")
 OUT_DIR = os.path.join(HERE, "_ref")
 LIB = os.path.join(OUT_DIR, "libref_binom.so")
 
