@@ -5,7 +5,10 @@
 
 namespace gpda {
 
-constexpr int kThreads = 256;       // threads per CTA of the MC kernels
+#ifndef GPDA_THREADS
+#define GPDA_THREADS 256
+#endif
+constexpr int kThreads = GPDA_THREADS;   // threads per CTA of the MC kernels (a multiple of 64)
 #ifndef GPDA_MIN_BLOCKS
 #define GPDA_MIN_BLOCKS 4
 #endif
