@@ -190,6 +190,11 @@ int ensure_scratch(gpda_ctx *c, int P) {
 #ifndef GPDA_TILE_UNITS
 #define GPDA_TILE_UNITS 2048
 #endif
+// photon mode: launch the Monte-Carlo kernel as a programmatic dependent of
+// the binomial-table kernel (1) or after it completes (0)
+#ifndef GPDA_PDL
+#define GPDA_PDL 1
+#endif
 
 int tile_bursts(const gpda_ctx *c, int mode, int S, int64_t nb, int P) {
     int tb = 0;
@@ -234,6 +239,12 @@ int prepare_launch(gpda_ctx *c, int mode, int P, int n, const float *params) {
     const int nbins = c->model.nbins;
     CK(cudaMemcpyAsync(c->dParams, c->hParams, sizeof(DevParams) * P, cudaMemcpyHostToDevice, c->stream));
     CK(cudaEventRecord(c->params_ev, c->stream));
+    // resets first, then the tables right before the Monte-Carlo kernel,
+    // which runs as their programmatic dependent (GPDA_PDL); the kernel's
+    // events enclose both
+    CK(cudaMemsetAsync(c->dHist, 0, sizeof(unsigned long long) * (size_t)P * nbins, c->stream));
+    CK(cudaMemsetAsync(c->dWork, 0, 2 * sizeof(unsigned int), c->stream));
+    CK(cudaEventRecord(c->k0, c->stream));
     if (mode == GPDA_MODE_PHOTON) {
         const size_t ntab = (size_t)P * n;
         if (ntab > c->cap_tab) {
@@ -249,7 +260,6 @@ int prepare_launch(gpda_ctx *c, int mode, int P, int n, const float *params) {
         CK(launch_binom_tables(c->dParams, P, n, c->dCdf, c->dGuide, c->stream));
         c->launches += 1;
     }
-    CK(cudaMemsetAsync(c->dHist, 0, sizeof(unsigned long long) * (size_t)P * nbins, c->stream));
     c->last_P = P;
     c->last_chi2 = false;
     return GPDA_OK;
@@ -308,14 +318,13 @@ int range_args(gpda_ctx *c, int mode, int P, int n, int64_t b0, int64_t b1, int 
 // range_args), timed by the context's events.
 int enqueue_range(gpda_ctx *c, int mode, int P, int n, int64_t b0, int64_t b1, int S,
                   uint64_t seed, int32_t *dUnit, bool with_chi2, const unsigned int *abort_flag) {
-    CK(cudaMemsetAsync(c->dWork, 0, 2 * sizeof(unsigned int), c->stream));
     if (b1 == b0) return GPDA_OK;
     PdaArgs a;
     int grid = 0;
     int rc = range_args(c, mode, P, n, b0, b1, S, seed, dUnit, with_chi2, abort_flag, a, grid);
     if (rc) return rc;
     size_t dyn = (mode == GPDA_MODE_PHOTON) ? sizeof(float) * kSmemCapFloats : 0;
-    CK(cudaEventRecord(c->k0, c->stream));
+    a.pdl = (mode == GPDA_MODE_PHOTON && GPDA_PDL) ? 1 : 0;   // right after the tables
     CK(launch_pda(mode, a, grid, dyn, c->stream));
     CK(cudaEventRecord(c->k1, c->stream));
     c->timed = true;
@@ -1111,8 +1120,7 @@ int32_t gpda_run_host(gpda_ctx *c, int32_t mode, int32_t P, int32_t n, const flo
             a.wT = c->dT;
             a.wOffIdx = c->dOffIdx;
             a.wOff = c->dOff;
-            CK(cudaMemsetAsync(c->dWork, 0, 2 * sizeof(unsigned int), c->stream));
-            CK(cudaEventRecord(c->k0, c->stream));
+            a.pdl = GPDA_PDL;       // right after the tables (prepare_launch)
             cudaError_t e = launch_pda(kModePhotonDirect, a, grid, sizeof(float) * kSmemCapFloats, c->stream);
             if (e != cudaSuccess) {
                 cudaStreamSynchronize(c->stream);

@@ -103,6 +103,9 @@ struct PdaArgs {
     // the staged span's last vector is read element by element up to the
     // tile's last photon instead of as one 16-byte load
     int32_t exact_offsets;
+    // photon mode: launched as a programmatic dependent of the binomial-table
+    // kernel just before it on the same stream (launch_pda)
+    int32_t pdl;
     // direct reads (launch mode kModePhotonDirect, one parameter set, vflag
     // set): each CTA stages its tile from the caller's page-locked host
     // arrays hN, hT, hOffIdx, hOff (device-mapped; naturally aligned, hOff

@@ -621,6 +621,9 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) pda_kernel(const PdaArgs
                 __syncthreads();
             }
         }
+        // photon mode: the binomial tables of the kernel launched before
+        // this one (a no-op unless this launch is a programmatic dependent)
+        if (kPhoton) asm volatile("griddepcontrol.wait;" ::: "memory");
         // photon mode: one dwell segment per step; a lane whose unit is
         // finished takes the tile's next unit at once
         Unit U;
@@ -910,6 +913,10 @@ binom_table_kernel(const DevParams *params, int P, int n_states, float *cdf_all,
     const int lane = threadIdx.x & 31;
     const int wl = threadIdx.x >> 5;
     const int64_t rid = (int64_t)blockIdx.x * kTableWarps + wl;
+    // the Monte-Carlo kernel that follows may start now (programmatic
+    // dependent launch): it stages its first tile while the rows are built
+    // and waits for them (griddepcontrol.wait) before its first draw
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     const int64_t total = (int64_t)P * n_states * (kTableN + 1);
     if (rid >= total) return;                       // whole warps leave together
     const int nn = kTableN - (int)(rid % (kTableN + 1));
@@ -1073,6 +1080,21 @@ const void *pda_kernel_fn(int mode) {
 }
 
 cudaError_t launch_pda(int mode, const PdaArgs &a, int grid, size_t dyn_smem, cudaStream_t st) {
+    if (mode != 0 && a.pdl) {
+        // programmatic dependent launch after the binomial-table kernel
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((unsigned)grid);
+        cfg.blockDim = dim3(kThreads);
+        cfg.dynamicSmemBytes = dyn_smem;
+        cfg.stream = st;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr[0].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        if (mode == kModePhotonDirect) return cudaLaunchKernelEx(&cfg, pda_kernel<2>, a);
+        return cudaLaunchKernelEx(&cfg, pda_kernel<1>, a);
+    }
     if (mode == 0) pda_kernel<0><<<grid, kThreads, dyn_smem, st>>>(a);
     else if (mode == kModePhotonDirect) pda_kernel<2><<<grid, kThreads, dyn_smem, st>>>(a);
     else pda_kernel<1><<<grid, kThreads, dyn_smem, st>>>(a);
