@@ -687,7 +687,8 @@ def main():
             "frac": alu_achieved / alu_peak, "traffic": traffic,
             "peak_kind": f"lane-issue rate, 152 SMs x 128 lanes x {sm_mhz:.0f} MHz (median SM clock "
                          "sampled in the timed region); MEASURED_PEAKS.json holds no ALU peak",
-            "kernel": "pda_kernel<1>", "kernel_ms": kavg_ms,
+            "kernel": "pda_kernel<1>, timed with the binomial-table kernel it overlaps "
+                      "(programmatic dependent launch)", "kernel_ms": kavg_ms,
             "ops_per_unit": cost["ops"],
             "cost_model": {"draws": cost["draws"], "search": cost["search"],
                            "segments_per_unit": cost["segments"], "mean_photons": cost["mean_photons"],
