@@ -37,6 +37,19 @@ namespace gpda {
 // direct reads: host-memory loads each thread keeps in flight while staging
 constexpr int kStageBatch = 4;
 
+// occupancy mode: units per thread per round (trajectories and background of
+// all of them, then one barrier and the regrouped binomial splits)
+#ifndef GPDA_OCC_ROUND
+#define GPDA_OCC_ROUND 1
+#endif
+constexpr int kOccRound = GPDA_OCC_ROUND;
+// with one unit per thread per round: a CTA barrier between the
+// trajectories and the background draws (1)
+#ifndef GPDA_OCC_MIDSYNC
+#define GPDA_OCC_MIDSYNC 1
+#endif
+constexpr int kOccEntries = kOccRound * kThreads;
+
 // Unsigned division by an invariant divisor (Granlund & Montgomery, "Division
 // by invariant integers using multiplication", PLDI 1994, fig. 4.1): for
 // 1 <= d < 2^31, l = ceil(log2 d) and m = floor(2^32 (2^l - d) / d) + 1 give
@@ -330,8 +343,8 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) pda_kernel(const PdaArgs
     __shared__ int s_staged;
     __shared__ int s_next;
     __shared__ float s_inv[kInvTable];
-    __shared__ uint32_t s_ent[10][kThreads];     // occupancy mode: sorted splits
-    __shared__ int s_nf, s_nb;
+    __shared__ uint32_t s_ent[10][kOccEntries];  // occupancy mode: sorted splits
+    __shared__ int s_nf[2], s_nb[2];             // their counts, alternating by round
     const int tid = threadIdx.x;
     const int lane = tid & 31;
     // a rejected burst store: nothing to simulate. One read per CTA (the flag
@@ -538,86 +551,99 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) pda_kernel(const PdaArgs
             if (__syncthreads_or(bad != 0u)) continue;
         }
         if (MODE == 0) {
-            // Rounds of kThreads units. 1. each thread runs its unit's
-            // trajectory; 2. background, and the binomial split classified
-            // by sampler (the inversion BINV for n min(p,q) < 10, else BTRD):
-            // its arguments and remaining random words go to a shared list,
-            // BINV from the front, BTRD from the back; 3. thread t finishes
-            // entry t, so at most one warp mixes the two samplers. Every
-            // unit continues its own Philox stream: results do not depend
-            // on which thread finishes it.
-            for (int r0 = 0; r0 < units; r0 += kThreads) {
-                if (tid == 0) { s_nf = 0; s_nb = 0; }
-                const int u = r0 + tid;
-                const bool act = u < units;
-                Unit U;
-                int bin = -1;
-                if (act) {
-                    unit_begin(U, u, a.S, sdiv(s_Sm, s_Sl), tb0, sN, sT, a.seed, pw);
-                    if (!U.done)
-                        while (!traj_occ(U, sp, a.r0, lim)) {
+            // Rounds of kOccRound units per thread. 1. each thread runs its
+            // unit's trajectory; 2. background, and the binomial split
+            // classified by sampler (the inversion BINV for n min(p,q) < 10,
+            // else BTRD): its arguments and remaining random words go to a
+            // shared list, BINV from the front, BTRD from the back (1 and 2
+            // repeat for the thread's next unit of the round); 3. thread t
+            // finishes entries t, t + kThreads, ..., so that few warps mix
+            // the two samplers. Every unit continues its own Philox stream:
+            // results do not depend on which thread finishes it. The counts
+            // of round r live in s_nf/s_nb[r & 1]; the other pair is cleared
+            // during the round.
+            if (tid == 0) { s_nf[0] = s_nf[1] = 0; s_nb[0] = s_nb[1] = 0; }
+            __syncthreads();
+            int rr = 0;
+            for (int r0 = 0; r0 < units; r0 += kOccEntries, ++rr) {
+                const int c = rr & 1;
+                for (int k = 0; k < kOccRound; ++k) {
+                    const int u = r0 + k * kThreads + tid;
+                    const bool act = u < units;
+                    Unit U;
+                    int bin = -1;
+                    if (act) {
+                        unit_begin(U, u, a.S, sdiv(s_Sm, s_Sl), tb0, sN, sT, a.seed, pw);
+                        if (!U.done)
+                            while (!traj_occ(U, sp, a.r0, lim)) {
+                            }
+                    }
+                    if (kOccRound == 1 && GPDA_OCC_MIDSYNC) __syncthreads();
+                    if (act && !U.done) {
+                        const float eeff = (U.Tb > 0.0f) ? U.acc / U.Tb : sp.E[U.st];
+                        U.r.align();
+                        int sig;
+                        const int ba = background_occ(U.r, U.Nb, a.bg_a * U.Tb, a.bg_d * U.Tb, &sig, lim, s_inv);
+                        const float pe = eps_of(eeff, a.gamma, a.ct);
+                        if (sig <= 0 || !(pe > 0.0f)) U.A = ba;
+                        else if (pe >= 1.0f) U.A = ba + sig;
+                        else {
+                            const float pp = pe > 0.5f ? 1.0f - pe : pe;
+                            const bool inv_sampler = (float)sig * pp < 10.0f;
+                            const int slot = inv_sampler ? atomicAdd(&s_nf[c], 1)
+                                                         : kOccEntries - 1 - atomicAdd(&s_nb[c], 1);
+                            s_ent[0][slot] = (uint32_t)u;
+                            s_ent[1][slot] = (uint32_t)sig;
+                            s_ent[2][slot] = (uint32_t)ba;
+                            s_ent[3][slot] = __float_as_uint(pe);
+                            s_ent[4][slot] = U.r.blk;
+                            s_ent[5][slot] = (uint32_t)U.r.idx;
+                            s_ent[6][slot] = U.r.w0;
+                            s_ent[7][slot] = U.r.w1;
+                            s_ent[8][slot] = U.r.w2;
+                            s_ent[9][slot] = U.r.w3;
+                            U.A = -2;                   // finished in phase 3
                         }
+                    }
+                    if (act && U.A != -2) {
+                        const int64_t b = tb0 + U.lb;
+                        if (a.unit_out) a.unit_out[((int64_t)p * (a.b1 - a.b0) + (b - a.b0)) * a.S + U.s] = U.A;
+                        if (U.Nb > 0 && U.A >= 0) {
+                            unsigned v = div_by((unsigned)U.A * (unsigned)a.nbins, sNm[U.lb], sNl[U.lb]);
+                            bin = v >= (unsigned)a.nbins ? a.nbins - 1 : (int)v;
+                        }
+                    }
+                    hist_add_warp(sh, bin);
                 }
                 __syncthreads();
-                if (act && !U.done) {
-                    const float eeff = (U.Tb > 0.0f) ? U.acc / U.Tb : sp.E[U.st];
-                    U.r.align();
-                    int sig;
-                    const int ba = background_occ(U.r, U.Nb, a.bg_a * U.Tb, a.bg_d * U.Tb, &sig, lim, s_inv);
-                    const float pe = eps_of(eeff, a.gamma, a.ct);
-                    if (sig <= 0 || !(pe > 0.0f)) U.A = ba;
-                    else if (pe >= 1.0f) U.A = ba + sig;
-                    else {
-                        const float pp = pe > 0.5f ? 1.0f - pe : pe;
-                        const bool inv_sampler = (float)sig * pp < 10.0f;
-                        const int slot = inv_sampler ? atomicAdd(&s_nf, 1) : kThreads - 1 - atomicAdd(&s_nb, 1);
-                        s_ent[0][slot] = (uint32_t)u;
-                        s_ent[1][slot] = (uint32_t)sig;
-                        s_ent[2][slot] = (uint32_t)ba;
-                        s_ent[3][slot] = __float_as_uint(pe);
-                        s_ent[4][slot] = U.r.blk;
-                        s_ent[5][slot] = (uint32_t)U.r.idx;
-                        s_ent[6][slot] = U.r.w0;
-                        s_ent[7][slot] = U.r.w1;
-                        s_ent[8][slot] = U.r.w2;
-                        s_ent[9][slot] = U.r.w3;
-                        U.A = -2;                   // finished in phase 3
-                    }
-                }
-                if (act && U.A != -2) {
-                    const int64_t b = tb0 + U.lb;
-                    if (a.unit_out) a.unit_out[((int64_t)p * (a.b1 - a.b0) + (b - a.b0)) * a.S + U.s] = U.A;
-                    if (U.Nb > 0 && U.A >= 0) {
-                        unsigned v = div_by((unsigned)U.A * (unsigned)a.nbins, sNm[U.lb], sNl[U.lb]);
+                const int nf = s_nf[c], nbk = s_nb[c];
+                if (tid == 0) { s_nf[c ^ 1] = 0; s_nb[c ^ 1] = 0; }
+                for (int k = 0; k < kOccRound; ++k) {
+                    const int e = k * kThreads + tid;
+                    int bin = -1;
+                    if (e < nf || e >= kOccEntries - nbk) {
+                        const int ue = (int)s_ent[0][e];
+                        const int sig = (int)s_ent[1][e];
+                        const int ba = (int)s_ent[2][e];
+                        const float pe = __uint_as_float(s_ent[3][e]);
+                        const Divisor dS = sdiv(s_Sm, s_Sl);
+                        const int lb = (int)div_by((uint32_t)ue, dS.m, dS.l), ss = ue - lb * a.S;
+                        Rng r;
+                        r.init(a.seed, pw, (uint32_t)(tb0 + lb), (uint32_t)ss);
+                        r.blk = s_ent[4][e];
+                        r.idx = (int)s_ent[5][e];
+                        r.w0 = s_ent[6][e];
+                        r.w1 = s_ent[7][e];
+                        r.w2 = s_ent[8][e];
+                        r.w3 = s_ent[9][e];
+                        const int A = binom(r, sig, pe, lim, s_inv) + ba;
+                        const int64_t b = tb0 + lb;
+                        if (a.unit_out) a.unit_out[((int64_t)p * (a.b1 - a.b0) + (b - a.b0)) * a.S + ss] = A;
+                        unsigned v = div_by((unsigned)A * (unsigned)a.nbins, sNm[lb], sNl[lb]);
                         bin = v >= (unsigned)a.nbins ? a.nbins - 1 : (int)v;
                     }
+                    hist_add_warp(sh, bin);
                 }
-                hist_add_warp(sh, bin);
-                __syncthreads();
-                bin = -1;
-                const int nf = s_nf, nbk = s_nb;
-                if (tid < nf || tid >= kThreads - nbk) {
-                    const int ue = (int)s_ent[0][tid];
-                    const int sig = (int)s_ent[1][tid];
-                    const int ba = (int)s_ent[2][tid];
-                    const float pe = __uint_as_float(s_ent[3][tid]);
-                    const Divisor dS = sdiv(s_Sm, s_Sl);
-                    const int lb = (int)div_by((uint32_t)ue, dS.m, dS.l), ss = ue - lb * a.S;
-                    Rng r;
-                    r.init(a.seed, pw, (uint32_t)(tb0 + lb), (uint32_t)ss);
-                    r.blk = s_ent[4][tid];
-                    r.idx = (int)s_ent[5][tid];
-                    r.w0 = s_ent[6][tid];
-                    r.w1 = s_ent[7][tid];
-                    r.w2 = s_ent[8][tid];
-                    r.w3 = s_ent[9][tid];
-                    const int A = binom(r, sig, pe, lim, s_inv) + ba;
-                    const int64_t b = tb0 + lb;
-                    if (a.unit_out) a.unit_out[((int64_t)p * (a.b1 - a.b0) + (b - a.b0)) * a.S + ss] = A;
-                    unsigned v = div_by((unsigned)A * (unsigned)a.nbins, sNm[lb], sNl[lb]);
-                    bin = v >= (unsigned)a.nbins ? a.nbins - 1 : (int)v;
-                }
-                hist_add_warp(sh, bin);
                 __syncthreads();
             }
         }
