@@ -69,6 +69,22 @@ std::mutex g_setup_mu;
 
 constexpr int kSmemCapFloats = 8192;  // same photon staging capacity as the context-based path
 
+// The parameter tables reach the scratch as kernel arguments: a launch takes
+// its own copy of them, so nothing refers to this call's stack once it has
+// returned (a cudaMemcpyAsync from a pageable stack array would). 24 tables
+// make 27,264 bytes, within the 32,764-byte argument limit of sm_70 and later.
+constexpr int kParamsPerLaunch = 24;
+struct ParamBatch {
+    DevParams p[kParamsPerLaunch];
+};
+static_assert(sizeof(ParamBatch) <= 32764, "kernel argument limit");
+
+__global__ void noalloc_params_kernel(const ParamBatch b, int count, DevParams *dst) {
+    const uint32_t *src = reinterpret_cast<const uint32_t *>(b.p);
+    uint32_t *d = reinterpret_cast<uint32_t *>(dst);
+    for (int i = threadIdx.x; i < count * kParamWords; i += blockDim.x) d[i] = src[i];
+}
+
 int setup_device(int dev, DeviceSetup **out) {
     std::lock_guard<std::mutex> lock(g_setup_mu);
     DeviceSetup &s = g_setup[dev];
@@ -127,20 +143,31 @@ extern "C" int32_t gpda_run_pda_noalloc(const gpda_model *m, int32_t mode, int32
     int rc = setup_device(dev, &su);
     if (rc) return rc;
 
-    // parameter tables: built on this thread's stack, copied into the scratch
-    DevParams host_params[kNoAllocMaxP];
+    // parameter tables: built on this thread's stack in batches, each batch
+    // passed by value to a copy kernel (see ParamBatch); all are checked
+    // before anything is enqueued
+    ParamBatch batch[(kNoAllocMaxP + kParamsPerLaunch - 1) / kParamsPerLaunch];
     const size_t stride = (size_t)n_states * (n_states + 1);
     for (int p = 0; p < P; ++p) {
-        int r = build_params(n_states, params + stride * p, mm.gamma, mm.crosstalk, true, &host_params[p]);
+        int r = build_params(n_states, params + stride * p, mm.gamma, mm.crosstalk, true,
+                             &batch[p / kParamsPerLaunch].p[p % kParamsPerLaunch]);
         if (r == -2) return GPDA_ERR_SINGULAR;
         if (r != 0) return GPDA_ERR_ARG;
     }
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     NoAllocScratch *sc = su->scratch;
     const int nbins = mm.nbins;
-    // pageable source: the copy is staged before cudaMemcpyAsync returns
-    if (cudaMemcpyAsync(sc->params, host_params, sizeof(DevParams) * P, cudaMemcpyHostToDevice, st) != cudaSuccess ||
-        cudaMemsetAsync(&sc->work, 0, sizeof(unsigned int), st) != cudaSuccess ||
+    for (int p0 = 0; p0 < P; p0 += kParamsPerLaunch) {
+        int count = std::min(kParamsPerLaunch, P - p0);
+        DevParams *dst = sc->params + p0;
+        void *kargs[] = {&batch[p0 / kParamsPerLaunch], &count, &dst};
+        if (cudaLaunchKernel(reinterpret_cast<const void *>(noalloc_params_kernel), dim3(1), dim3(256), kargs,
+                             0, st) != cudaSuccess) {
+            cudaGetLastError();
+            return GPDA_ERR_CUDA;
+        }
+    }
+    if (cudaMemsetAsync(&sc->work, 0, sizeof(unsigned int), st) != cudaSuccess ||
         cudaMemsetAsync(&sc->limit_hits, 0, sizeof(unsigned long long), st) != cudaSuccess ||
         cudaMemsetAsync(hist, 0, sizeof(uint64_t) * (size_t)P * nbins, st) != cudaSuccess) {
         cudaGetLastError();

@@ -244,7 +244,8 @@ int32_t gpda_expected_grad(gpda_ctx *ctx, int32_t P, int32_t n_states, const flo
  * gpda_upload_bursts accepts; not re-validated here) and writes P*nbins
  * counts into the DEVICE array hist (zeroed first); with ohist/chi2 (device,
  * nbins floats / P doubles) it also writes the reduced chi-square. params is
- * a HOST array of P*n(n+1) floats. Arrays are naturally aligned and offsets
+ * a HOST array of P*n(n+1) floats, read before the call returns (its tables
+ * reach the device as kernel arguments). Arrays are naturally aligned and offsets
  * starts on a 16-byte boundary (GPDA_ERR_ARG otherwise); offsets may be
  * exactly off_idx[B] floats long. Allocates nothing: its scratch is a fixed
  * array of about 21 MB inside the library, held by every device that loads
