@@ -179,16 +179,24 @@ int ensure_scratch(gpda_ctx *c, int P) {
 }
 
 // Bursts per work item for a launch over nb bursts and P parameter sets: the
-// tuned value for (mode, S), else ~2048 units (photon mode: tiles whose
-// offsets fit the shared-memory staging). Occupancy mode then caps it so that
-// the launch has at least 4 work items per resident CTA (a single parameter
-// set otherwise leaves CTAs idle at the end), down to one round of kThreads
-// units. Photon mode keeps its tiles: there a lane takes the tile's next unit
-// as soon as its own is done, and tiles of fewer units per lane measured
-// slower than the end-of-launch imbalance they remove. GPDA_TILE_UNITS (a
-// build option) sets the ~2048.
+// tuned value for (mode, S), else ~GPDA_TILE_UNITS units (photon mode: tiles
+// whose offsets fit the shared-memory staging). Occupancy mode then caps it
+// so that the launch has at least 4 work items per resident CTA (a single
+// parameter set otherwise leaves CTAs idle at the end), down to one round of
+// kThreads units. Photon mode keeps its tiles: there a lane takes the tile's
+// next unit as soon as its own is done, and tiles of fewer units per lane
+// measured slower than the end-of-launch imbalance they remove. Direct reads
+// of host arrays (gpda_run_host) take ~GPDA_TILE_UNITS_DIRECT units and no
+// tuned value: each CTA's staging there waits on the host link, and smaller
+// tiles spread those waits. Measured on photon_3state (100 samples per
+// burst): 3,200 units (32 bursts) against 2,048 (21), resident kernel 0.652
+// -> 0.642 ms, direct reads 0.742 -> 0.752 ms per call; occupancy mode on 64
+// parameter sets, untuned, 15.60 -> 15.04 ms. The same bits at any tile.
 #ifndef GPDA_TILE_UNITS
-#define GPDA_TILE_UNITS 2048
+#define GPDA_TILE_UNITS 3200
+#endif
+#ifndef GPDA_TILE_UNITS_DIRECT
+#define GPDA_TILE_UNITS_DIRECT 2048
 #endif
 // photon mode: launch the Monte-Carlo kernel as a programmatic dependent of
 // the binomial-table kernel (1) or after it completes (0)
@@ -196,12 +204,12 @@ int ensure_scratch(gpda_ctx *c, int P) {
 #define GPDA_PDL 1
 #endif
 
-int tile_bursts(const gpda_ctx *c, int mode, int S, int64_t nb, int P) {
+int tile_bursts(const gpda_ctx *c, int mode, int S, int64_t nb, int P, bool direct = false) {
     int tb = 0;
     for (const auto &t : c->tuned)
-        if (t[0] == mode && t[1] == S) tb = t[2];
+        if (!direct && t[0] == mode && t[1] == S) tb = t[2];
     if (tb == 0) {
-        tb = (GPDA_TILE_UNITS + S - 1) / S;
+        tb = ((direct ? GPDA_TILE_UNITS_DIRECT : GPDA_TILE_UNITS) + S - 1) / S;
         if (mode == GPDA_MODE_PHOTON && c->mean_N > 0.0) {
             int fit = (int)(0.6 * kSmemCapFloats / c->mean_N);
             tb = std::min(tb, std::max(fit, 1));
@@ -1109,6 +1117,14 @@ int32_t gpda_run_host(gpda_ctx *c, int32_t mode, int32_t P, int32_t n, const flo
                 c->B = 0;
                 return rc;
             }
+            a.tile_b = tile_bursts(c, mode, S, B, P, true);
+            if ((B + a.tile_b - 1) / a.tile_b > (int64_t)INT32_MAX) {
+                cudaStreamSynchronize(c->stream);
+                c->B = 0;
+                return fail(c, GPDA_ERR_ARG, "too many work items");
+            }
+            a.ntiles = (int)((B + a.tile_b - 1) / a.tile_b);
+            a.n_items = a.ntiles;   // one parameter set
             grid = (int)std::min<int64_t>(a.n_items, (int64_t)c->num_sms * c->blocks_per_sm[kModePhotonDirect]);
             a.vflag = c->dFlag;
             a.nph = nph;

@@ -37,11 +37,6 @@ namespace gpda {
 // direct reads: host-memory loads each thread keeps in flight while staging
 constexpr int kStageBatch = 4;
 
-// photon mode: guide entries prefetched per segment (0: none)
-#ifndef GPDA_GUIDE_PREFETCH
-#define GPDA_GUIDE_PREFETCH 0
-#endif
-
 // occupancy mode: units per thread per round (trajectories and background of
 // all of them, then one barrier and the regrouped binomial splits)
 #ifndef GPDA_OCC_ROUND
@@ -206,25 +201,6 @@ __device__ __forceinline__ bool step_pho(Unit &U, const DevParams &P, const floa
     if (last) { hi = U.Nb; dt = U.Tb - U.t; }
     else { hi = lower_bound(offs, U.lo, U.Nb, tn); dt = tn - U.t; }
     int nk = hi - U.lo;
-#if GPDA_GUIDE_PREFETCH > 0
-    // the binomial's guide entry is read after the background pair, at the
-    // row of the signal count nk - (background), with the block's last word:
-    // prefetch it for the likeliest few signal counts so that the load that
-    // follows finds it in L1 (no effect on any result)
-    if (nk > 0 && nk <= kTableN && !(P.V[st] > 0.0f)) {
-        const float ub = (float)((U.r.w3 >> 8) + 1u) * 5.9604644775390625e-08f;
-#pragma unroll
-        for (int g = 0; g < GPDA_GUIDE_PREFETCH; ++g) {
-            const int ng = nk - g;
-            if (ng >= 1) {
-                int jg = (int)(ub * (float)(ng + 1));
-                if (jg > ng) jg = ng;
-                const GuideEntry *ga = guide_p + st * kTableRows + ng * (ng + 1) / 2 + jg;
-                asm volatile("prefetch.global.L1 [%0];" ::"l"(ga));
-            }
-        }
-    }
-#endif
     if (nk > 0) {
         int sig;
         int ba = background_pair(U.r, nk, dt, bgc, &sig, lim, inv);
