@@ -206,7 +206,7 @@ __device__ __forceinline__ bool step_pho(Unit &U, const DevParams &P, const floa
         int ba = background_pair(U.r, nk, dt, bgc, &sig, lim, inv);
         if (P.V[st] > 0.0f) {
             float ek = eps_of(broaden(U.r, P.E[st], r0, P.V[st]), g, ct);
-            U.A += binom(U.r, sig, ek, lim, inv) + ba;
+            U.A += binom<false>(U.r, sig, ek, lim, inv) + ba;
         } else {
             U.A += binom_table(U.r, sig, P, st, cdf_p, guide_p, lim, inv) + ba;
         }
@@ -831,7 +831,7 @@ __global__ void __launch_bounds__(kThreads) rc_kernel(const RcArgs a) {
                         f_i = floorf((float)((double)(f_if - bgd - bga) + 0.5));
                     }
                     float de = broaden(r, sp.E[si], r0, sp.V[si]);
-                    ai = binom(r, (int)f_i, de, lim, s_inv);
+                    ai = binom<false>(r, (int)f_i, de, lim, s_inv);
                     break;
                 }
                 if (ddx > 0) sdd = 1;
