@@ -53,13 +53,13 @@ HELD_OUT_SEED = 0x0B5E
 # gsmfretda_gb300/roofline.py evaluated on the workload (its mean segments per
 # unit from the stationary jump flux of the parameter set, its mean photons).
 # Thread instructions the kernel executes per unit, from one ncu capture of a
-# full launch of pda_kernel<1> on this workload (524.7 M warp instructions x
-# 18.66 active threads per instruction / 1e7 units;
+# full launch of pda_kernel<1> on this workload (507.3 M warp instructions x
+# 19.23 active threads per instruction / 1e7 units;
 # profiles/pda_kernel_photon_3state.txt).
-ISSUED_INST_PER_UNIT = 979.1
-# DRAM bytes (read + write) of that launch (67.84 MB + 0.83 MB); the
+ISSUED_INST_PER_UNIT = 975.6
+# DRAM bytes (read + write) of that launch (67.85 MB + 0.77 MB); the
 # algorithmic figure is computed live below.
-NCU_TRAFFIC_BYTES = 68.67e6
+NCU_TRAFFIC_BYTES = 68.62e6
 
 
 def parse():
@@ -662,7 +662,7 @@ def main():
     hbm_peak, peak_kind, sm_max = peaks()
     achieved_gbs = alg_bytes / (kavg_ms * 1e-3) / 1e9
     from gsmfretda_gb300 import roofline as rl
-    cost = rl.photon_ops_breakdown(n, args, bs.N, bs.T)
+    cost = rl.photon_ops_breakdown(n, args, bs.N, bs.T, md["bg_a"] + md["bg_d"])
     clk = clocks.summary()
     sm_mhz = clk.get("sm_mhz") or sm_max
     alu_peak = rl.lane_peak_gops(sm_mhz)               # FP32/INT32 lane-ops per s, in Gop/s
@@ -691,10 +691,12 @@ def main():
                       "(programmatic dependent launch)", "kernel_ms": kavg_ms,
             "ops_per_unit": cost["ops"],
             "cost_model": {"draws": cost["draws"], "search": cost["search"],
+                           "background": cost["background"],
                            "segments_per_unit": cost["segments"], "mean_photons": cost["mean_photons"],
+                           "background_photons_per_unit": cost["background_photons"],
                            "linear_scan_not_counted": cost["linear_scan"],
-                           "frac_if_linear_scan_counted": unit_rate * (cost["draws"] + cost["linear_scan"])
-                           / 1e9 / alu_peak,
+                           "frac_if_linear_scan_counted": unit_rate * (cost["draws"] + cost["background"]
+                                                                       + cost["linear_scan"]) / 1e9 / alu_peak,
                            "source": "gsmfretda_gb300/roofline.py"},
             "issued": {"inst_per_unit": ISSUED_INST_PER_UNIT, "achieved": alu_issued,
                        "frac": alu_issued / alu_peak,

@@ -10,15 +10,23 @@ counted with fixed costs per operation:
     BINOMIAL        40  ops per binomial draw (BTRD, or a table inversion)
     SEARCH_STEP      4  ops per bisection step over a burst's sorted arrival
                         offsets (midpoint, load, compare, select)
+    EXP             16  FP32 ops per exponential (e^-lam of a Poisson inversion)
+    POISSON_STEP     4  ops per step of the Poisson inversion (compare,
+                        subtract, two multiplies)
+    SPLIT_TRIAL      3  ops per background photon split into acceptor/donor
 
 and the draws of the photon-by-photon model: with D dwell segments per unit,
 1 + 2D + 4 + D random words (initial state; jump and dwell per segment;
-background; one binomial per segment), D logarithms and D binomials, and one
+background; one binomial per segment), D logarithms and D binomials, one
 bisection of the burst's N sorted offsets per segment that ends inside the
-burst (the last segment takes the photons left):
+burst (the last segment takes the photons left), and the segment's Poisson
+background pair: an exponential, T + 1 inversion steps for a count T, and T
+split trials, where the counts of a unit's segments add up to lam_B = (bg_a +
+bg_d) T on average over a burst of duration T:
 
     ops(D, N) = PHILOX_WORD (5 + 3 D) + (LOG + BINOMIAL) D
-                + SEARCH_STEP (D - 1) log2(N + 1).
+                + SEARCH_STEP (D - 1) log2(N + 1)
+                + EXP D + POISSON_STEP (lam_B + D) + SPLIT_TRIAL lam_B.
 
 A linear scan that compares every photon once (PHOTON_COMPARE = 2 ops per
 photon, 2 N per unit) is the other way to assign photons; it is reported
@@ -35,6 +43,9 @@ PHILOX_WORD = 25
 LOG = 16
 BINOMIAL = 40
 SEARCH_STEP = 4
+EXP = 16
+POISSON_STEP = 4
+SPLIT_TRIAL = 3
 PHOTON_COMPARE = 2
 
 
@@ -71,23 +82,27 @@ def mean_segments(n, args, T):
     return 1.0 + flux * float(np.mean(np.asarray(T, dtype=np.float64)))
 
 
-def photon_ops_breakdown(n, args, N, T):
+def photon_ops_breakdown(n, args, N, T, bg=0.0):
     """The cost model's terms per unit on bursts with photon counts N and
-    durations T: draws (Philox words, logarithms, binomials), search (the
-    bisections that assign photons to segments), their sum, the linear-scan
-    alternative (not counted) and D."""
+    durations T, background rate bg = bg_a + bg_d (per second): draws (Philox
+    words, logarithms, binomials), search (the bisections that assign photons
+    to segments), background (the segments' Poisson pairs), their sum, the
+    linear-scan alternative (not counted), D and lam_B."""
     D = mean_segments(n, args, T)
     Nbar = float(np.mean(np.asarray(N, dtype=np.float64)))
+    lam = float(bg) * float(np.mean(np.asarray(T, dtype=np.float64)))
     draws = PHILOX_WORD * (5.0 + 3.0 * D) + (LOG + BINOMIAL) * D
     search = SEARCH_STEP * (D - 1.0) * float(np.log2(Nbar + 1.0))
-    return {"draws": draws, "search": search, "ops": draws + search,
-            "linear_scan": PHOTON_COMPARE * Nbar, "segments": D, "mean_photons": Nbar}
+    background = EXP * D + POISSON_STEP * (lam + D) + SPLIT_TRIAL * lam if bg > 0.0 else 0.0
+    return {"draws": draws, "search": search, "background": background,
+            "ops": draws + search + background, "linear_scan": PHOTON_COMPARE * Nbar,
+            "segments": D, "mean_photons": Nbar, "background_photons": lam}
 
 
-def photon_ops_per_unit(n, args, N, T):
+def photon_ops_per_unit(n, args, N, T, bg=0.0):
     """(ops per unit, D) of the photon-by-photon model on bursts with photon
-    counts N and durations T."""
-    b = photon_ops_breakdown(n, args, N, T)
+    counts N and durations T and background rate bg."""
+    b = photon_ops_breakdown(n, args, N, T, bg)
     return b["ops"], b["segments"]
 
 

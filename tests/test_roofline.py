@@ -57,3 +57,17 @@ def test_photon_ops_per_unit_formula():
     assert abs(b["draws"] + b["search"] - ops) < 1e-9
     assert abs(b["linear_scan"] - 2 * Nbar) < 1e-9
 
+
+
+def test_background_term_counts_the_poisson_pairs():
+    """bg_a + bg_d = 2,300 /s over the photon_3state bursts: an exponential
+    and (lam + 1) inversion steps per segment, a split trial per background
+    photon; no term without background."""
+    bs, n, args, md, S = synth.photon_3state(B=2000, seed=2)
+    bg = md["bg_a"] + md["bg_d"]
+    b = rl.photon_ops_breakdown(n, args, bs.N, bs.T, bg)
+    D, lam = b["segments"], bg * float(np.mean(bs.T.astype(np.float64)))
+    assert abs(b["background_photons"] - lam) < 1e-9
+    assert abs(b["background"] - (16 * D + 4 * (lam + D) + 3 * lam)) < 1e-9
+    assert abs(b["ops"] - (b["draws"] + b["search"] + b["background"])) < 1e-9
+    assert rl.photon_ops_breakdown(n, args, bs.N, bs.T)["background"] == 0.0
