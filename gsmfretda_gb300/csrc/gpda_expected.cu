@@ -40,6 +40,11 @@ namespace gpda {
 namespace {
 
 constexpr int kExpThreads = 256;
+// 1: the adjoint keeps its per-unit statistics and gradient sums in the
+// thread's shared-memory columns (see exp_walk); 0: in registers
+#ifndef GPDA_ADJ_SMEM
+#define GPDA_ADJ_SMEM 1
+#endif
 constexpr float kMassCut = 0x1p-24f;
 constexpr uint32_t kExpBgBlock = 0x80000000u;   // above any trajectory block (< 2^15)
 
@@ -134,21 +139,37 @@ struct ExpUnit {
     int cnt[NS][NS];    // jumps from -> to
 };
 
+// Where the adjoint's trajectory statistics live: STATS_REG in U.D / U.cnt
+// (registers), STATS_SMEM in the thread's own columns of shared arrays,
+// scnt[(i * NS + j) * kExpThreads] (jumps i -> j) and sD[i * kExpThreads]
+// (time in state i): one shared-memory update per segment instead of NS * NS
+// predicated register updates, and the registers freed for occupancy. The
+// same integer counts and the same FP32 sums in the same order either way.
+constexpr int STATS_NONE = 0, STATS_REG = 1, STATS_SMEM = 2;
+
 // The trajectory of one unit under (skeleton theta0, dwells theta), then the
 // background; returns false when the burst has no photons.
-template <int NS, bool STATS>
+template <int NS, int STATS>
 __device__ __forceinline__ bool exp_walk(const ExpParams &P, Rng &r, int Nb, float Tb, float bga,
                                          float bgd, ExpUnit<NS> &U, int &sig, int &ba, int &lim,
-                                         const float *sinv) {
+                                         const float *sinv, int *scnt = nullptr, float *sD = nullptr) {
     U.acc = 0.0f;
     U.lw = 0.0f;
     U.dtl = 0.0f;
-    if (STATS) {
+    if (STATS == STATS_REG) {
 #pragma unroll
         for (int i = 0; i < NS; ++i) {
             U.D[i] = 0.0f;
 #pragma unroll
             for (int j = 0; j < NS; ++j) U.cnt[i][j] = 0;
+        }
+    }
+    if (STATS == STATS_SMEM) {
+#pragma unroll
+        for (int i = 0; i < NS; ++i) {
+            sD[i * kExpThreads] = 0.0f;
+#pragma unroll
+            for (int j = 0; j < NS; ++j) scnt[(i * NS + j) * kExpThreads] = 0;
         }
     }
     float t = 0.0f;
@@ -163,13 +184,14 @@ __device__ __forceinline__ bool exp_walk(const ExpParams &P, Rng &r, int Nb, flo
         } else {
             ns = jump_draw(P.jump_cdf + st * 4, NS, st, us);
             U.lw += P.lw_jump[st * 4 + ns];
-            if (STATS) {
+            if (STATS == STATS_REG) {
 #pragma unroll
                 for (int i = 0; i < NS; ++i)
 #pragma unroll
                     for (int j = 0; j < NS; ++j)
                         if (i == st && j == ns) U.cnt[i][j] += 1;
             }
+            if (STATS == STATS_SMEM) scnt[(st * NS + ns) * kExpThreads] += 1;
         }
         st = ns;
         if (!(Tb > 0.0f)) break;
@@ -185,11 +207,12 @@ __device__ __forceinline__ bool exp_walk(const ExpParams &P, Rng &r, int Nb, flo
             U.dtl = dt;
             break;
         }
-        if (STATS) {
+        if (STATS == STATS_REG) {
 #pragma unroll
             for (int i = 0; i < NS; ++i)
                 if (i == st) U.D[i] += dt;
         }
+        if (STATS == STATS_SMEM) sD[st * kExpThreads] += dt;
         t = tn;
     }
     U.sm = st;
@@ -347,7 +370,7 @@ __global__ void __launch_bounds__(kExpThreads) exp_fwd_kernel(const ExpArgs a) {
         r.init(a.seed, (uint32_t)p, (uint32_t)b, (uint32_t)s);
         ExpUnit<NS> U;
         int sig, ba;
-        if (!exp_walk<NS, false>(sP, r, Nb, Tb, a.bg_a, a.bg_d, U, sig, ba, lim, s_inv)) continue;
+        if (!exp_walk<NS, STATS_NONE>(sP, r, Nb, Tb, a.bg_a, a.bg_d, U, sig, ba, lim, s_inv)) continue;
         const float eeff = (Tb > 0.0f) ? U.acc / Tb : sP.E[U.sm];
         const float W = expf_(U.lw);
         const float pe = eps_p(eeff, a.gamma, a.ct);
@@ -445,9 +468,12 @@ __global__ void __launch_bounds__(kExpChi2Threads) exp_chi2_kernel(const ExpArgs
 template <int NS, bool TAPE>
 __global__ void __launch_bounds__(kExpThreads) exp_adj_kernel(const ExpArgs a) {
     constexpr int NG = NS + NS * (NS - 1);
+    constexpr bool kSm = GPDA_ADJ_SMEM != 0;
     __shared__ float s_inv[kInvTable];
     __shared__ float s_g[kExpMaxBins];
     __shared__ float s_red[NG][kExpThreads];
+    __shared__ int s_cnt[kSm ? NS * NS : 1][kSm ? kExpThreads : 1];
+    __shared__ float s_D[kSm ? NS : 1][kSm ? kExpThreads : 1];
     __shared__ ExpParams sP;
     const int tid = threadIdx.x;
     const int p = blockIdx.y;
@@ -455,9 +481,16 @@ __global__ void __launch_bounds__(kExpThreads) exp_adj_kernel(const ExpArgs a) {
     if (tid < 128) reinterpret_cast<float *>(&sP)[tid] = reinterpret_cast<const float *>(a.params + p)[tid];
     if (tid < a.nbins) s_g[tid] = a.g[(size_t)p * a.nbins + tid];
     __syncthreads();
-    float gacc[NG];
+    // the gradient sums: registers, or (kSm) the thread's column of s_red
+    float gacc[kSm ? 1 : NG];
 #pragma unroll
-    for (int k = 0; k < NG; ++k) gacc[k] = 0.0f;
+    for (int k = 0; k < NG; ++k) {
+        if (kSm) s_red[k][tid] = 0.0f;
+        else gacc[k] = 0.0f;
+    }
+    auto gadd = [&](int k, float v) -> float & { return kSm ? s_red[k][tid] : gacc[kSm ? 0 : k]; };
+    int *const cnt_col = kSm ? &s_cnt[0][tid] : nullptr;
+    float *const d_col = kSm ? &s_D[0][tid] : nullptr;
     const int64_t units = a.B * (int64_t)a.S;
     const int64_t stride = (int64_t)a.nblk_adj * kExpThreads;
     const bool narrow = units + stride <= (int64_t)0xffffffffu;
@@ -472,7 +505,9 @@ __global__ void __launch_bounds__(kExpThreads) exp_adj_kernel(const ExpArgs a) {
         r.init(a.seed, (uint32_t)p, (uint32_t)b, (uint32_t)s);
         ExpUnit<NS> U;
         int sig, ba;
-        if (!exp_walk<NS, true>(sP, r, Nb, Tb, a.bg_a, a.bg_d, U, sig, ba, lim, s_inv)) continue;
+        if (!exp_walk<NS, kSm ? STATS_SMEM : STATS_REG>(sP, r, Nb, Tb, a.bg_a, a.bg_d, U, sig, ba, lim,
+                                                        s_inv, cnt_col, d_col))
+            continue;
         const bool timed = Tb > 0.0f;
         const float eeff = timed ? U.acc / Tb : sP.E[U.sm];
         const float W = expf_(U.lw);
@@ -499,12 +534,17 @@ __global__ void __launch_bounds__(kExpThreads) exp_adj_kernel(const ExpArgs a) {
         const float WG = W * G;
         // d / d E_s: occupancy fraction of state s
         const float invT = timed ? 1.0f / Tb : 0.0f;
+        auto Dof = [&](int i) -> float { return kSm ? d_col[i * kExpThreads] : U.D[kSm ? 0 : i]; };
+        auto cntof = [&](int i, int j) -> int {
+            return kSm ? cnt_col[(i * NS + j) * kExpThreads] : U.cnt[kSm ? 0 : i][kSm ? 0 : j];
+        };
 #pragma unroll
         for (int i = 0; i < NS; ++i) {
             float occ;
-            if (timed) occ = (U.D[i] + (i == U.sm ? U.dtl : 0.0f)) * invT;
+            if (timed) occ = (Dof(i) + (i == U.sm ? U.dtl : 0.0f)) * invT;
             else occ = (i == U.sm) ? 1.0f : 0.0f;
-            gacc[i] = fmaf(HE, occ, gacc[i]);
+            float &g = gadd(i, 0.0f);
+            g = fmaf(HE, occ, g);
         }
         // d / d ln K(l, i), rate i -> l: skeleton score and dwell pathwise term
         const float Esm = sP.E[U.sm];
@@ -516,17 +556,20 @@ __global__ void __launch_bounds__(kExpThreads) exp_adj_kernel(const ExpArgs a) {
                 const int idx = l * (NS - 1) + (i < l ? i : i - 1);
                 int nout = 0;
 #pragma unroll
-                for (int j = 0; j < NS; ++j) nout += U.cnt[i][j];
+                for (int j = 0; j < NS; ++j) nout += cntof(i, j);
                 const float pj = sP.pj[i * 4 + l];
-                float score = sP.dlnpi[U.s0 * 12 + idx] + (float)U.cnt[i][l] - (float)nout * pj;
-                float path = -pj * U.D[i] * (sP.E[i] - Esm) * invT;
-                gacc[NS + idx] = fmaf(WG, score, fmaf(HE, path, gacc[NS + idx]));
+                float score = sP.dlnpi[U.s0 * 12 + idx] + (float)cntof(i, l) - (float)nout * pj;
+                float path = -pj * Dof(i) * (sP.E[i] - Esm) * invT;
+                float &g = gadd(NS + idx, 0.0f);
+                g = fmaf(WG, score, fmaf(HE, path, g));
             }
         }
     }
     if (lim) atomicAdd(a.limit_hits, (unsigned long long)lim);
+    if (!kSm) {
 #pragma unroll
-    for (int k = 0; k < NG; ++k) s_red[k][tid] = gacc[k];
+        for (int k = 0; k < NG; ++k) s_red[k][tid] = gacc[kSm ? 0 : k];
+    }
     __syncthreads();
     const int warp = tid >> 5, lane = tid & 31;
     double *out = a.gpart + ((size_t)p * a.nblk_adj + blockIdx.x) * kExpGrad;
