@@ -95,8 +95,17 @@ struct Rng {
 #endif
     }
     // uniform on (0,1]: ((x >> 8) + 1) * 2^-24, exact
-    __device__ __forceinline__ float u01() {
-        return (float)((next() >> 8) + 1u) * 5.9604644775390625e-08f;
+    __device__ __forceinline__ float u01() { return u01_of(next()); }
+    __device__ __forceinline__ static float u01_of(uint32_t x) {
+        return (float)((x >> 8) + 1u) * 5.9604644775390625e-08f;
+    }
+    // the next block, generated out of line, for a caller that takes its four
+    // words itself (the same words as four next() calls from a fresh block)
+    __device__ __forceinline__ uint4 block() {
+        const uint4 v = philox_block(blk, c1, c2, c3, k0, k1);
+        blk += 1u;
+        idx = 4;
+        return v;
     }
 };
 

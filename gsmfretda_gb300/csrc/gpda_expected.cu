@@ -45,6 +45,11 @@ constexpr int kExpThreads = 256;
 #ifndef GPDA_ADJ_SMEM
 #define GPDA_ADJ_SMEM 1
 #endif
+// the trajectory's segments in pairs from one Philox block (see exp_walk):
+// 0 off, 1 with the out-of-line block generator, 2 with it inline
+#ifndef GPDA_EXP_PAIRS
+#define GPDA_EXP_PAIRS 2
+#endif
 constexpr float kMassCut = 0x1p-24f;
 constexpr uint32_t kExpBgBlock = 0x80000000u;   // above any trajectory block (< 2^15)
 
@@ -174,6 +179,63 @@ __device__ __forceinline__ bool exp_walk(const ExpParams &P, Rng &r, int Nb, flo
     }
     float t = 0.0f;
     int st = 0;
+#if GPDA_EXP_PAIRS
+    // Every segment draws two words (state, dwell), so a Philox block covers
+    // two segments: the words are taken in place, the same draws in the same
+    // order as one next() per draw. Returns true when the trajectory ends.
+    auto step = [&](int seg, uint32_t xs, uint32_t xu) -> bool {
+        const float us = Rng::u01_of(xs);
+        int ns;
+        if (seg == 0) {
+            ns = cat_draw(P.init_cdf, NS, us);
+            U.s0 = ns;
+            U.lw += P.lw_init[ns];
+        } else {
+            ns = jump_draw(P.jump_cdf + st * 4, NS, st, us);
+            U.lw += P.lw_jump[st * 4 + ns];
+            if (STATS == STATS_REG) {
+#pragma unroll
+                for (int i = 0; i < NS; ++i)
+#pragma unroll
+                    for (int j = 0; j < NS; ++j)
+                        if (i == st && j == ns) U.cnt[i][j] += 1;
+            }
+            if (STATS == STATS_SMEM) scnt[(st * NS + ns) * kExpThreads] += 1;
+        }
+        st = ns;
+        if (!(Tb > 0.0f)) return true;
+        const float u = Rng::u01_of(xu);
+        float tau = (P.kexit[st] > 0.0f) ? (-logf_pos(u)) * P.inv_kexit[st] : kInf;
+        float tn = t + tau;
+        bool cut = seg == kMaxSeg - 1;
+        bool last = !(tn < Tb) || cut;
+        if (cut && tn < Tb) lim += 1;
+        float dt = last ? Tb - t : tn - t;
+        U.acc = fmaf(dt, P.E[st], U.acc);
+        if (last) {
+            U.dtl = dt;
+            return true;
+        }
+        if (STATS == STATS_REG) {
+#pragma unroll
+            for (int i = 0; i < NS; ++i)
+                if (i == st) U.D[i] += dt;
+        }
+        if (STATS == STATS_SMEM) sD[st * kExpThreads] += dt;
+        t = tn;
+        return false;
+    };
+    for (int seg = 0; seg < kMaxSeg; seg += 2) {
+#if GPDA_EXP_PAIRS == 2
+        const uint4 w = philox_block_inline(r.blk, r.c1, r.c2, r.c3, r.k0, r.k1);
+        r.blk += 1u;
+#else
+        const uint4 w = r.block();
+#endif
+        if (step(seg, w.x, w.y) || step(seg + 1, w.z, w.w)) break;
+    }
+    if (false)
+#endif
     for (int seg = 0; seg < kMaxSeg; ++seg) {
         const float us = r.u01();
         int ns;

@@ -243,6 +243,35 @@ __device__ __forceinline__ bool traj_occ(Unit &U, const DevParams &P, float r0, 
     return false;
 }
 
+// traj_occ for parameter sets without distance broadening (every segment
+// draws exactly two words, state and dwell), with the segment's two words
+// given: the caller takes them from one Philox block per pair of segments,
+// the same draws in the same order as traj_occ's two u01() calls.
+__device__ __forceinline__ bool traj_occ_words(Unit &U, const DevParams &P, int &lim, uint32_t xs,
+                                               uint32_t xu) {
+    const int st = next_state(U, P, Rng::u01_of(xs));
+    U.st = st;
+    if (!(U.Tb > 0.0f)) return true;
+    float u = Rng::u01_of(xu);
+    float tau = (P.kexit[st] > 0.0f) ? (-logf_pos(u)) * P.inv_kexit[st] : kInf;
+    float tn = U.t + tau;
+    bool cut = U.seg == kMaxSeg - 1;
+    bool last = !(tn < U.Tb) || cut;
+    if (cut && tn < U.Tb) lim += 1;
+    float dt = last ? U.Tb - U.t : tn - U.t;
+    U.acc = fmaf(dt, P.E[st], U.acc);
+    if (last) return true;
+    U.t = tn;
+    U.seg += 1;
+    return false;
+}
+
+// 1: occupancy trajectories without broadening take their segments in pairs
+// from one block (traj_occ_words)
+#ifndef GPDA_OCC_PAIRS
+#define GPDA_OCC_PAIRS 1
+#endif
+
 // The occupancy split draws its background through out-of-line Poisson
 // samplers: measured 3-5 % faster there (the split runs once per unit),
 // while the photon step keeps them inline (out of line costs it 40 %).
@@ -574,9 +603,21 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) pda_kernel(const PdaArgs
                     int bin = -1;
                     if (act) {
                         unit_begin(U, u, a.S, sdiv(s_Sm, s_Sl), tb0, sN, sT, a.seed, pw);
-                        if (!U.done)
-                            while (!traj_occ(U, sp, a.r0, lim)) {
+                        if (!U.done) {
+                            if (GPDA_OCC_PAIRS && !sp.anyV) {
+                                for (;;) {
+                                    const uint4 w = philox_block_inline(U.r.blk, U.r.c1, U.r.c2, U.r.c3,
+                                                                        U.r.k0, U.r.k1);
+                                    U.r.blk += 1u;
+                                    if (traj_occ_words(U, sp, lim, w.x, w.y) ||
+                                        traj_occ_words(U, sp, lim, w.z, w.w))
+                                        break;
+                                }
+                            } else {
+                                while (!traj_occ(U, sp, a.r0, lim)) {
+                                }
                             }
+                        }
                     }
                     if (kOccRound == 1 && GPDA_OCC_MIDSYNC) __syncthreads();
                     if (act && !U.done) {
