@@ -109,6 +109,29 @@ struct Rng {
     }
 };
 
+// Unsigned division by an invariant divisor (Granlund & Montgomery, "Division
+// by invariant integers using multiplication", PLDI 1994, fig. 4.1): for
+// 1 <= d < 2^31, l = ceil(log2 d) and m = floor(2^32 (2^l - d) / d) + 1 give
+// n / d = (t + ((n - t) >> min(l, 1))) >> max(l - 1, 0), t = umulhi(m, n),
+// for every 32-bit n. The kernels divide by the samples per burst (unit ->
+// burst, sample), by a burst's photon count (its bin) and by the bin count.
+struct Divisor {
+    uint32_t m, l;
+};
+
+__device__ __forceinline__ Divisor divisor_of(uint32_t d) {
+    const uint32_t l = (d > 1u) ? 32u - (uint32_t)__clz((int)(d - 1u)) : 0u;
+    const uint64_t num = (uint64_t)((1ull << l) - d) << 32;
+    return Divisor{(uint32_t)(num / d + 1ull), l};
+}
+
+__device__ __forceinline__ uint32_t div_by(uint32_t n, uint32_t m, uint32_t l) {
+    const uint32_t t = __umulhi(m, n);
+    const uint32_t sh1 = l > 0u ? 1u : 0u;
+    const uint32_t sh2 = l > 0u ? l - 1u : 0u;
+    return (t + ((n - t) >> sh1)) >> sh2;
+}
+
 // ---------------------------------------------------------------- FP32 math
 // Written from the mathematics: log by 2*atanh((m-1)/(m+1)) series, exp by
 // Taylor series after k*ln2 reduction, cos(2*pi*u) by the sine series.

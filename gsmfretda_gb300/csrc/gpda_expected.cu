@@ -125,8 +125,8 @@ __device__ __forceinline__ float binom_pmf(int n, int m, float p, float q) {
 // first acceptor count a with floor(a * nbins / N) >= b. The store holds
 // N <= 2^21 photons per burst and this path nbins <= 64, so every product
 // below stays under 2^27: 32-bit unsigned division is exact.
-__device__ __forceinline__ int bin_start(int b, int N, int nbins) {
-    return (int)(((unsigned)b * (unsigned)N + (unsigned)(nbins - 1)) / (unsigned)nbins);
+__device__ __forceinline__ int bin_start(int b, int N, int nbins, Divisor dn) {
+    return (int)div_by((unsigned)b * (unsigned)N + (unsigned)(nbins - 1), dn.m, dn.l);
 }
 
 __device__ __forceinline__ int bin_of(int a, int N, int nbins) {
@@ -302,7 +302,7 @@ __device__ __forceinline__ float eps_dp(float e, float g, float ct) {
 // the upward part). Inside a bin the number of terms is known, so the term
 // loop carries no bin test; the mass cut is tested every 4 terms.
 template <bool WANT_X, class F>
-__device__ __forceinline__ void binom_bins(int Nb, int sig, int ba, float p, int nbins,
+__device__ __forceinline__ void binom_bins(int Nb, int sig, int ba, float p, int nbins, Divisor dn,
                                            const float *inv, F &&flush) {
     if (sig <= 0 || !(p > 0.0f)) {
         flush(bin_of(ba, Nb, nbins), 1.0f, 0.0f);
@@ -330,7 +330,7 @@ __device__ __forceinline__ void binom_bins(int Nb, int sig, int ba, float p, int
             int b = bin_of(ba + x, Nb, nbins);
             bool more = true;
             while (more) {
-                int first = bin_start(b, Nb, nbins) - ba;
+                int first = bin_start(b, Nb, nbins, dn) - ba;
                 if (first < 0) first = 0;
                 int cnt = x - first + 1;
                 float run = 0.0f, runx = 0.0f;
@@ -366,7 +366,7 @@ __device__ __forceinline__ void binom_bins(int Nb, int sig, int ba, float p, int
         int b = bm;
         bool more = true;
         while (more) {
-            int last = (b < nbins - 1) ? bin_start(b + 1, Nb, nbins) - 1 - ba : sig;
+            int last = (b < nbins - 1) ? bin_start(b + 1, Nb, nbins, dn) - 1 - ba : sig;
             if (last > sig) last = sig;
             int cnt = last - x + 1;
             float run = 0.0f, runx = 0.0f;
@@ -422,9 +422,10 @@ __global__ void __launch_bounds__(kExpThreads) exp_fwd_kernel(const ExpArgs a) {
     int lim = 0;
     float *row = sh_rows + tid;
     const int nb2 = 2 * a.nbins;
+    const Divisor dn = divisor_of((uint32_t)a.nbins), dS = divisor_of((uint32_t)a.S);
     for (int64_t u = (int64_t)blockIdx.x * kExpThreads + tid; u < units; u += stride) {
-        // (32-bit division whenever the unit count allows)
-        const int b = narrow ? (int)((uint32_t)u / (uint32_t)a.S) : (int)(u / a.S);
+        // (32-bit division by the invariant S whenever the unit count allows)
+        const int b = narrow ? (int)div_by((uint32_t)u, dS.m, dS.l) : (int)(u / a.S);
         const int s = (int)(u - (int64_t)b * a.S);
         const int Nb = __ldg(a.N + b);
         const float Tb = __ldg(a.T + b);
@@ -440,7 +441,7 @@ __global__ void __launch_bounds__(kExpThreads) exp_fwd_kernel(const ExpArgs a) {
         // contiguous range), zeros around them
         float *t = TAPE ? a.tape + (size_t)p * nb2 * a.units_p + u : nullptr;
         int bmin = a.nbins, bmax = -1;
-        binom_bins<TAPE>(Nb, sig, ba, pe, a.nbins, a.inv, [&](int bin, float m, float mx) {
+        binom_bins<TAPE>(Nb, sig, ba, pe, a.nbins, dn, a.inv, [&](int bin, float m, float mx) {
             row[bin * kExpThreads] += W * m;
             if (TAPE) {
                 __stcs(t + (size_t)bin * a.units_p, m);
@@ -557,9 +558,10 @@ __global__ void __launch_bounds__(kExpThreads) exp_adj_kernel(const ExpArgs a) {
     const int64_t stride = (int64_t)a.nblk_adj * kExpThreads;
     const bool narrow = units + stride <= (int64_t)0xffffffffu;
     int lim = 0;
+    const Divisor dn = divisor_of((uint32_t)a.nbins), dS = divisor_of((uint32_t)a.S);
     for (int64_t u = (int64_t)blockIdx.x * kExpThreads + tid; u < units; u += stride) {
-        // (32-bit division whenever the unit count allows)
-        const int b = narrow ? (int)((uint32_t)u / (uint32_t)a.S) : (int)(u / a.S);
+        // (32-bit division by the invariant S whenever the unit count allows)
+        const int b = narrow ? (int)div_by((uint32_t)u, dS.m, dS.l) : (int)(u / a.S);
         const int s = (int)(u - (int64_t)b * a.S);
         const int Nb = __ldg(a.N + b);
         const float Tb = __ldg(a.T + b);
@@ -583,7 +585,7 @@ __global__ void __launch_bounds__(kExpThreads) exp_adj_kernel(const ExpArgs a) {
                 GX = fmaf(gb, __ldcs(t + (size_t)(a.nbins + bin) * a.units_p), GX);
             }
         } else {
-            binom_bins<true>(Nb, sig, ba, pe, a.nbins, a.inv, [&](int bin, float m, float mx) {
+            binom_bins<true>(Nb, sig, ba, pe, a.nbins, dn, a.inv, [&](int bin, float m, float mx) {
                 const float gb = s_g[bin];
                 G = fmaf(gb, m, G);
                 GX = fmaf(gb, mx, GX);

@@ -50,29 +50,6 @@ constexpr int kOccRound = GPDA_OCC_ROUND;
 #endif
 constexpr int kOccEntries = kOccRound * kThreads;
 
-// Unsigned division by an invariant divisor (Granlund & Montgomery, "Division
-// by invariant integers using multiplication", PLDI 1994, fig. 4.1): for
-// 1 <= d < 2^31, l = ceil(log2 d) and m = floor(2^32 (2^l - d) / d) + 1 give
-// n / d = (t + ((n - t) >> min(l, 1))) >> max(l - 1, 0), t = umulhi(m, n),
-// for every 32-bit n. The kernels divide by the samples per burst (unit ->
-// burst, sample) and by a burst's photon count (its bin) once per unit.
-struct Divisor {
-    uint32_t m, l;
-};
-
-__device__ __forceinline__ Divisor divisor_of(uint32_t d) {
-    const uint32_t l = (d > 1u) ? 32u - (uint32_t)__clz((int)(d - 1u)) : 0u;
-    const uint64_t num = (uint64_t)((1ull << l) - d) << 32;
-    return Divisor{(uint32_t)(num / d + 1ull), l};
-}
-
-__device__ __forceinline__ uint32_t div_by(uint32_t n, uint32_t m, uint32_t l) {
-    const uint32_t t = __umulhi(m, n);
-    const uint32_t sh1 = l > 0u ? 1u : 0u;
-    const uint32_t sh2 = l > 0u ? l - 1u : 0u;
-    return (t + ((n - t) >> sh1)) >> sh2;
-}
-
 // a divisor kept in shared memory, read at each use (so that it does not hold
 // two registers across the simulation loop)
 __device__ __forceinline__ Divisor sdiv(const uint32_t &m, const uint32_t &l) {
