@@ -568,6 +568,30 @@ __device__ __forceinline__ int background(Rng &r, int navail, float lam_a, float
     return B[0];
 }
 
+// background() through out-of-line Poisson samplers (the same draws): the
+// occupancy split, which runs once per unit, measured 3-5 % faster with it;
+// the photon step keeps them inline (out of line costs it 40 %).
+static __device__ __noinline__ int pinv_ool(Rng &r, float lam, int &lim, const float *inv) {
+    return pinv(r, lam, lim, inv);
+}
+static __device__ __noinline__ int ptrs_ool(Rng &r, float lam, int &lim) { return ptrs(r, lam, lim); }
+
+__device__ __forceinline__ int background_occ(Rng &r, int navail, float lam_a, float lam_d, int *sig,
+                                              int &lim, const float *inv) {
+    int B[2];
+    int avail = navail;
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+        const float lam = c == 0 ? lam_a : lam_d;
+        int x = !(lam > 0.0f) ? 0 : (lam < 10.0f) ? pinv_ool(r, lam, lim, inv) : ptrs_ool(r, lam, lim);
+        if (x > avail) x = (int)floorf((float)avail * r.u01());
+        B[c] = x;
+        avail -= x;
+    }
+    *sig = avail;
+    return B[0];
+}
+
 // Background of one photon-mode segment as a pair: T = A + D ~ Poisson(lam),
 // lam = (bg_a + bg_d) dt, split by A ~ Binomial(T, pa), pa = bg_a / (bg_a +
 // bg_d), which has the law of independent Poisson(bg_a dt) and

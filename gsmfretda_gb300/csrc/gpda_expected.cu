@@ -45,6 +45,13 @@ constexpr int kExpThreads = 256;
 #ifndef GPDA_ADJ_SMEM
 #define GPDA_ADJ_SMEM 1
 #endif
+// 1: the unit's background draws through the out-of-line Poisson samplers
+// (background_occ: the same draws, a smaller kernel body; the 4-state adjoint
+// then needs 48 registers instead of 62). fit_4state gradient step 9.48 ->
+// 9.40 ms; Loader's pmf out of line as well measured 9.52 ms.
+#ifndef GPDA_EXP_BG_OOL
+#define GPDA_EXP_BG_OOL 1
+#endif
 // the trajectory's segments in pairs from one Philox block (see exp_walk):
 // 0 off, 1 with the out-of-line block generator, 2 with it inline
 #ifndef GPDA_EXP_PAIRS
@@ -281,7 +288,8 @@ __device__ __forceinline__ bool exp_walk(const ExpParams &P, Rng &r, int Nb, flo
     // the background comes from a fixed block, so that its counts do not
     // change when a dwell crosses the end of the burst
     r.seek(kExpBgBlock);
-    ba = background(r, Nb, bga * Tb, bgd * Tb, &sig, lim, sinv);
+    ba = GPDA_EXP_BG_OOL ? background_occ(r, Nb, bga * Tb, bgd * Tb, &sig, lim, sinv)
+                         : background(r, Nb, bga * Tb, bgd * Tb, &sig, lim, sinv);
     return Nb > 0;
 }
 

@@ -249,30 +249,6 @@ __device__ __forceinline__ bool traj_occ_words(Unit &U, const DevParams &P, int 
 #define GPDA_OCC_PAIRS 1
 #endif
 
-// The occupancy split draws its background through out-of-line Poisson
-// samplers: measured 3-5 % faster there (the split runs once per unit),
-// while the photon step keeps them inline (out of line costs it 40 %).
-static __device__ __noinline__ int pinv_ool(Rng &r, float lam, int &lim, const float *inv) {
-    return pinv(r, lam, lim, inv);
-}
-static __device__ __noinline__ int ptrs_ool(Rng &r, float lam, int &lim) { return ptrs(r, lam, lim); }
-
-__device__ __forceinline__ int background_occ(Rng &r, int navail, float lam_a, float lam_d, int *sig,
-                                              int &lim, const float *inv) {
-    int B[2];
-    int avail = navail;
-#pragma unroll
-    for (int c = 0; c < 2; ++c) {
-        const float lam = c == 0 ? lam_a : lam_d;
-        int x = !(lam > 0.0f) ? 0 : (lam < 10.0f) ? pinv_ool(r, lam, lim, inv) : ptrs_ool(r, lam, lim);
-        if (x > avail) x = (int)floorf((float)avail * r.u01());
-        B[c] = x;
-        avail -= x;
-    }
-    *sig = avail;
-    return B[0];
-}
-
 
 // warp-aggregated shared-memory histogram increment; all 32 lanes call it
 // (bin < 0: no count)
