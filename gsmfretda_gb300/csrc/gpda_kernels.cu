@@ -37,6 +37,11 @@ namespace gpda {
 // direct reads: host-memory loads each thread keeps in flight while staging
 constexpr int kStageBatch = 4;
 
+// occupancy mode: the same order (1); 64 population sets with untuned tiles
+// 13.66 -> 13.49 ms, the same bits
+#ifndef GPDA_LPT_OCC
+#define GPDA_LPT_OCC 1
+#endif
 // photon mode: each tile's bursts taken longest first (1). Measured on
 // photon_3state: MC kernel with its tables 0.640 -> 0.617 ms, gpda_run_host
 // 0.736 -> 0.704 ms per call, the same bits.
@@ -335,7 +340,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) pda_kernel(const PdaArgs
     __shared__ float s_inv[kInvTable];
     __shared__ uint32_t s_ent[10][kOccEntries];  // occupancy mode: sorted splits
     __shared__ int s_nf[2], s_nb[2];             // their counts, alternating by round
-    __shared__ uint8_t s_order[kMaxTileBursts];  // photon mode: the tile's bursts, longest first
+    __shared__ uint8_t s_order[kMaxTileBursts];  // the tile's bursts, longest first
     const int tid = threadIdx.x;
     const int lane = tid & 31;
     // a rejected burst store: nothing to simulate. One read per CTA (the flag
@@ -527,10 +532,12 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) pda_kernel(const PdaArgs
         const bool staged = kPhoton && s_staged;
         const uint32_t pw = a.pbase + (uint32_t)p;
 #if GPDA_LPT
-        // photon mode: the tile's bursts longest first (rank by duration,
-        // ties by index), so that the units left at the end of the tile are
-        // short ones; a unit's draws depend only on its (burst, sample)
-        if (kPhoton) {
+        // the tile's bursts longest first (rank by duration, ties by index):
+        // in photon mode the units left at the end of the tile are short
+        // ones; in occupancy mode each round's units have similar durations,
+        // so the round's barrier waits less for its longest trajectory. A
+        // unit's draws depend only on its (burst, sample).
+        if (kPhoton || GPDA_LPT_OCC) {
             for (int i = tid; i < nb; i += kThreads) {
                 const float ti = sT[i];
                 int rank = 0;
@@ -581,7 +588,8 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) pda_kernel(const PdaArgs
                     Unit U;
                     int bin = -1;
                     if (act) {
-                        unit_begin(U, u, a.S, sdiv(s_Sm, s_Sl), tb0, sN, sT, a.seed, pw);
+                        unit_begin(U, u, a.S, sdiv(s_Sm, s_Sl), tb0, sN, sT, a.seed, pw,
+                                   (GPDA_LPT && GPDA_LPT_OCC) ? s_order : nullptr);
                         if (!U.done) {
                             if (GPDA_OCC_PAIRS && !sp.anyV) {
                                 for (;;) {
@@ -647,7 +655,8 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) pda_kernel(const PdaArgs
                         const int ba = (int)s_ent[2][e];
                         const float pe = __uint_as_float(s_ent[3][e]);
                         const Divisor dS = sdiv(s_Sm, s_Sl);
-                        const int lb = (int)div_by((uint32_t)ue, dS.m, dS.l), ss = ue - lb * a.S;
+                        const int ke = (int)div_by((uint32_t)ue, dS.m, dS.l), ss = ue - ke * a.S;
+                        const int lb = (GPDA_LPT && GPDA_LPT_OCC) ? (int)s_order[ke] : ke;
                         Rng r;
                         r.init(a.seed, pw, (uint32_t)(tb0 + lb), (uint32_t)ss);
                         r.blk = s_ent[4][e];
