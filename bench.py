@@ -53,13 +53,13 @@ HELD_OUT_SEED = 0x0B5E
 # gsmfretda_gb300/roofline.py evaluated on the workload (its mean segments per
 # unit from the stationary jump flux of the parameter set, its mean photons).
 # Thread instructions the kernel executes per unit, from one ncu capture of a
-# full launch of pda_kernel<1> on this workload (507.3 M warp instructions x
-# 19.23 active threads per instruction / 1e7 units;
+# full launch of pda_kernel<1> on this workload (490.2 M warp instructions x
+# 19.96 active threads per instruction / 1e7 units;
 # profiles/pda_kernel_photon_3state.txt).
-ISSUED_INST_PER_UNIT = 975.6
-# DRAM bytes (read + write) of that launch (67.85 MB + 0.77 MB); the
+ISSUED_INST_PER_UNIT = 978.4
+# DRAM bytes (read + write) of that launch (67.84 MB + 0.73 MB); the
 # algorithmic figure is computed live below.
-NCU_TRAFFIC_BYTES = 68.62e6
+NCU_TRAFFIC_BYTES = 68.57e6
 
 
 def parse():
