@@ -538,12 +538,19 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) pda_kernel(const PdaArgs
         // so the round's barrier waits less for its longest trajectory. A
         // unit's draws depend only on its (burst, sample).
         if (kPhoton || GPDA_LPT_OCC) {
+            // rank on an integer key that orders every bit pattern (the
+            // float order for numbers, NaNs at the ends), so that the ranks
+            // are a permutation of 0..nb-1 whatever the durations hold
+            auto key = [](float t) {
+                const int k = __float_as_int(t);
+                return k ^ ((k >> 31) & 0x7fffffff);
+            };
             for (int i = tid; i < nb; i += kThreads) {
-                const float ti = sT[i];
+                const int ki = key(sT[i]);
                 int rank = 0;
                 for (int j = 0; j < nb; ++j) {
-                    const float tj = sT[j];
-                    rank += (tj > ti || (tj == ti && j < i)) ? 1 : 0;
+                    const int kj = key(sT[j]);
+                    rank += (kj > ki || (kj == ki && j < i)) ? 1 : 0;
                 }
                 s_order[rank] = (uint8_t)i;
             }
